@@ -1,0 +1,224 @@
+/*
+ * montblanc_gb300: C ABI of the GB300 (sm_103a) RIME v4 hot path.
+ *
+ * Every entry point takes plain device pointers (C-order arrays with the
+ * shapes of the reference's v4 array specification,
+ * montblanc/impl/rime/v4/config.py:131-247), a dims record that mirrors the
+ * reference's per-dimension constant data (global size, local size, lower
+ * and upper extent; montblanc/util/const_data.py:58-86), and a CUDA stream
+ * (cudaStream_t passed as void*; NULL = legacy default stream).  Complex
+ * arrays are interleaved (re, im); Jones matrices are row-major
+ * [00, 01, 10, 11].
+ *
+ * Nothing throws across the ABI: each call returns an mb_status and, on
+ * failure, sets a thread-local message readable with mb_last_error_string().
+ * No entry point allocates device memory; scratch space is reported by the
+ * *_workspace_size functions and passed in by the caller.  Launches are
+ * asynchronous on the given stream; no entry point synchronises the host.
+ */
+#ifndef MONTBLANC_GB300_H
+#define MONTBLANC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mb_status {
+  MB_OK = 0,
+  MB_ERR_NULL_PTR = 1,          /* a required pointer is NULL */
+  MB_ERR_BAD_SHAPE = 2,         /* inconsistent dimension sizes */
+  MB_ERR_BAD_EXTENT = 3,        /* extents outside [0, local] or local > global */
+  MB_ERR_UNSUPPORTED_DTYPE = 4, /* dtype is neither MB_FLOAT32 nor MB_FLOAT64 */
+  MB_ERR_CUDA = 5,              /* a CUDA runtime call failed */
+  MB_ERR_TIMEOUT = 6,           /* a bounded device-side wait gave up */
+  MB_ERR_WORKSPACE = 7,         /* workspace NULL, misaligned or too small */
+  MB_ERR_INVALID_ARG = 8,       /* any other invalid argument */
+  MB_ERR_UNSUPPORTED = 9        /* valid request this build cannot serve */
+} mb_status;
+
+typedef enum mb_dtype { MB_FLOAT32 = 0, MB_FLOAT64 = 1 } mb_dtype;
+
+/* Arithmetic form of the fused coherency sums.
+ * MB_MODE_NATIVE: CUDA-core arithmetic in the array dtype.
+ * MB_MODE_SPLIT_TF32 / MB_MODE_SPLIT_BF16: point sources as a per-(time,
+ * channel) complex GEMM on the tensor cores, operands split into hi + lo
+ * parts (3 products, FP32 accumulation); FLOAT32 data only.
+ * In every mode the phase argument and its range reduction run in FP64. */
+typedef enum mb_mode {
+  MB_MODE_NATIVE = 0,
+  MB_MODE_SPLIT_TF32 = 1,
+  MB_MODE_SPLIT_BF16 = 2
+} mb_mode;
+
+/* Option bits */
+#define MB_APPLY_WEIGHTS 0x1u /* weight chi^2 terms by weight_vector */
+#define MB_RESIDUALS 0x2u     /* write observed - model instead of model */
+
+typedef struct mb_dim {
+  uint32_t global_size;
+  uint32_t local_size;
+  uint32_t lower_extent;
+  uint32_t upper_extent;
+} mb_dim;
+
+/* Mirrors the reference's rime_const_data (montblanc/util/const_data.py).
+ * Strides use local_size; loops run over [0, upper_extent - lower_extent).
+ * For nsrc: lower_extent > 0 means "accumulate onto the partial sums held
+ * in model_vis", upper_extent < global_size means "store partial sums in
+ * model_vis and stop" (RimeSumCoherencies.py:185-190, 311-316). */
+typedef struct mb_dims {
+  mb_dim ntime, na, nbl, nchan, npol, npolchan;
+  mb_dim nsrc, npsrc, ngsrc, nssrc;
+  mb_dim beam_lw, beam_mh, beam_nud;
+} mb_dims;
+
+/* Scalar solver properties (montblanc/impl/rime/v4/config.py:54-69). */
+typedef struct mb_props {
+  double gauss_scale;
+  double two_pi_over_c;
+  double sigma_sqrd;
+  double beam_ll, beam_lm, beam_lfreq;
+  double beam_ul, beam_um, beam_ufreq;
+} mb_props;
+
+/* Library identification and error reporting. */
+const char* mb_version(void);
+const char* mb_last_error_string(void);
+const char* mb_status_string(mb_status s);
+
+/* ------------------------------------------------------------------------
+ * Per-stage entry points: the kernels behind the reference's pipeline nodes.
+ * ---------------------------------------------------------------------- */
+
+/* B_sqrt(nsrc, ntime, nchan, 4) from stokes(nsrc, ntime, 4),
+ * alpha(nsrc, ntime), frequency(nchan), ref_frequency(nchan).
+ * Replaces rime_jones_B_sqrt_{float,double}
+ * (montblanc/impl/rime/v4/gpu/RimeBSqrt.py:79-146) launched by
+ * RimeBSqrt.execute (RimeBSqrt.py:210-225). */
+mb_status mb_bsqrt(mb_dtype dtype, const mb_dims* dims, const void* stokes,
+                   const void* alpha, const void* frequency,
+                   const void* ref_frequency, void* B_sqrt, void* stream);
+
+/* jones(nsrc, ntime, na, nchan, 4) <- E beam from lm(nsrc, 2),
+ * parallactic_angles(ntime, na), point_errors(ntime, na, nchan, 2),
+ * antenna_scaling(na, nchan, 2), frequency(nchan),
+ * E_beam(beam_lw, beam_mh, beam_nud, 4).
+ * Replaces rime_jones_E_beam_{float,double}
+ * (montblanc/impl/rime/v4/gpu/RimeEBeam.py:138-368) launched by
+ * RimeEBeam.execute (RimeEBeam.py:442-460). */
+mb_status mb_ebeam(mb_dtype dtype, const mb_dims* dims, const mb_props* props,
+                   const void* lm, const void* parallactic_angles,
+                   const void* point_errors, const void* antenna_scaling,
+                   const void* frequency, const void* E_beam, void* jones,
+                   void* stream);
+
+/* jones <- jones . (K * B_sqrt) in place, K from uvw(ntime, na, 3),
+ * lm(nsrc, 2), frequency(nchan).
+ * Replaces rime_jones_EKBSqrt_{float,double}
+ * (montblanc/impl/rime/v4/gpu/RimeEKBSqrt.py:98-196) launched by
+ * RimeEKBSqrt.execute (RimeEKBSqrt.py:258-273). */
+mb_status mb_ekb_sqrt(mb_dtype dtype, const mb_dims* dims, const mb_props* props,
+                      const void* uvw, const void* lm, const void* frequency,
+                      const void* B_sqrt, void* jones, void* stream);
+
+/* Coherency sum over sources per (time, baseline, channel) with shapes,
+ * G-Jones, flags, model/residual output and chi^2 terms.
+ * gauss_shape(3, ngsrc) / sersic_shape(3, nssrc) may be NULL when empty.
+ * weight_vector may be NULL unless MB_APPLY_WEIGHTS is set.
+ * Replaces rime_sum_coherencies
+ * (montblanc/impl/rime/v4/gpu/RimeSumCoherencies.py:103-429) launched by
+ * RimeSumCoherencies.execute (RimeSumCoherencies.py:499-529). */
+mb_status mb_sum_coherencies(mb_dtype dtype, const mb_dims* dims,
+                             const mb_props* props, uint32_t options,
+                             const void* uvw, const void* gauss_shape,
+                             const void* sersic_shape, const void* frequency,
+                             const int32_t* antenna1, const int32_t* antenna2,
+                             const void* jones, const uint8_t* flag,
+                             const void* weight_vector,
+                             const void* observed_vis, const void* G_term,
+                             void* model_vis, void* chi_sqrd_result,
+                             void* stream);
+
+/* X2_out[0] = scale * sum of chi_sqrd_result over the active extents
+ * [0:ntime, 0:nbl, 0:nchan], summed in FP64 in a fixed order.
+ * Replaces pycuda.gpuarray.sum in RimeSumCoherencies.py:531-536 and
+ * RimeReduction.execute (montblanc/impl/rime/v5/gpu/RimeReduction.py:46-61);
+ * X2_out is a device pointer. */
+size_t mb_reduce_chi2_workspace_size(const mb_dims* dims);
+mb_status mb_reduce_chi2(mb_dtype dtype, const mb_dims* dims,
+                         const void* chi_sqrd_result, double scale,
+                         double* X2_out, void* workspace,
+                         size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Fused forward chi^2 and its adjoint (no per-antenna Jones array).
+ * ---------------------------------------------------------------------- */
+
+typedef struct mb_rime_inputs {
+  const void* uvw;                /* (ntime, na, 3) */
+  const int32_t* antenna1;        /* (ntime, nbl) */
+  const int32_t* antenna2;        /* (ntime, nbl) */
+  const void* frequency;          /* (nchan) */
+  const void* ref_frequency;      /* (nchan) */
+  const void* parallactic_angles; /* (ntime, na) */
+  const void* point_errors;       /* (ntime, na, nchan, 2) */
+  const void* antenna_scaling;    /* (na, nchan, 2) */
+  const void* E_beam;             /* (beam_lw, beam_mh, beam_nud, 4) complex */
+  const void* G_term;             /* (ntime, na, nchan, 4) complex */
+  const void* lm;                 /* (nsrc, 2) */
+  const void* stokes;             /* (nsrc, ntime, 4) */
+  const void* alpha;              /* (nsrc, ntime) */
+  const void* gauss_shape;        /* (3, ngsrc), NULL if ngsrc == 0 */
+  const void* sersic_shape;       /* (3, nssrc), NULL if nssrc == 0 */
+  const uint8_t* flag;            /* (ntime, nbl, nchan, 4) */
+  const void* weight_vector;      /* (ntime, nbl, nchan, 4), NULL unless weights */
+  const void* observed_vis;       /* (ntime, nbl, nchan, 4) complex */
+} mb_rime_inputs;
+
+/* Gradient outputs of mb_rime_adjoint, each in the input dtype and shape;
+ * any may be NULL.  Complex gradients are d/dRe + i d/dIm. */
+typedef struct mb_rime_grads {
+  void* lm;           /* (nsrc, 2) */
+  void* stokes;       /* (nsrc, ntime, 4) */
+  void* alpha;        /* (nsrc, ntime) */
+  void* gauss_shape;  /* (3, ngsrc) */
+  void* sersic_shape; /* (3, nssrc) */
+  void* G_term;       /* (ntime, na, nchan, 4) complex */
+} mb_rime_grads;
+
+/* Forward-only workspace (want_grad = 0) or forward + adjoint (1). */
+size_t mb_rime_workspace_size(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
+                              int want_grad);
+
+/* Forward: per-antenna E . K . sqrt(B) formed on the fly, coherency sums over
+ * all source types, G-Jones, flags, model/residual output (model_vis may be
+ * NULL), chi^2 terms (chi_sqrd_result may be NULL) and the chi^2 scalar
+ * (X2, device double, already divided by sigma_sqrd when weights are off).
+ * With want_grad = 1 it also leaves in the workspace what mb_rime_adjoint
+ * needs.  Fuses RimeBSqrt, RimeEBeam, RimeEKBSqrt, RimeSumCoherencies and the
+ * chi^2 reduction (montblanc/impl/rime/v4/RimeSolver.py:36-40). */
+mb_status mb_rime_forward(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
+                          const mb_props* props, uint32_t options,
+                          const mb_rime_inputs* in, void* model_vis,
+                          void* chi_sqrd_result, double* X2, int want_grad,
+                          void* workspace, size_t workspace_bytes,
+                          void* stream);
+
+/* Adjoint: grad_scale * d(chi^2)/d(parameters), using the state a preceding
+ * mb_rime_forward(..., want_grad = 1, same workspace) left behind.  K and E
+ * are recomputed, not stored.  No counterpart in the reference (it has no
+ * gradient). */
+mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
+                          const mb_props* props, uint32_t options,
+                          const mb_rime_inputs* in, double grad_scale,
+                          const mb_rime_grads* grads, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MONTBLANC_GB300_H */

@@ -1,0 +1,375 @@
+// Device-side building blocks shared by the stage kernels and the fused
+// kernels: complex / 2x2 Jones arithmetic and the per-(source, time,
+// antenna, channel) terms of the RIME v4 measurement equation.
+//
+// Conventions (identical to the reference's v4 arrays,
+// montblanc/impl/rime/v4/config.py:131-247): C order, complex values
+// interleaved (re, im), 2x2 Jones matrices stored row-major as
+// [00, 01, 10, 11] (XX, XY, YX, YY for visibilities).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/montblanc_gb300.h"
+
+namespace mb {
+
+constexpr double kLightSpeed = 299792458.0;  // montblanc/__init__.py:52-59
+constexpr double kPi = 3.141592653589793238462643383279502884;
+
+template <typename T> struct Vec2;
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+
+template <typename T>
+struct Cx {
+  T r, i;
+};
+
+template <typename T> __host__ __device__ __forceinline__ Cx<T> cx(T r, T i) { return Cx<T>{r, i}; }
+template <typename T> __device__ __forceinline__ Cx<T> operator+(Cx<T> a, Cx<T> b) { return {a.r + b.r, a.i + b.i}; }
+template <typename T> __device__ __forceinline__ Cx<T> operator-(Cx<T> a, Cx<T> b) { return {a.r - b.r, a.i - b.i}; }
+template <typename T> __device__ __forceinline__ Cx<T> operator*(Cx<T> a, T s) { return {a.r * s, a.i * s}; }
+template <typename T> __device__ __forceinline__ Cx<T> conj(Cx<T> a) { return {a.r, -a.i}; }
+// a * b
+template <typename T> __device__ __forceinline__ Cx<T> cmul(Cx<T> a, Cx<T> b) {
+  return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r};
+}
+// a * conj(b)
+template <typename T> __device__ __forceinline__ Cx<T> cmulc(Cx<T> a, Cx<T> b) {
+  return {a.r * b.r + a.i * b.i, a.i * b.r - a.r * b.i};
+}
+// acc += a * b
+template <typename T> __device__ __forceinline__ void cmac(Cx<T>& acc, Cx<T> a, Cx<T> b) {
+  acc.r = fma(a.r, b.r, fma(-a.i, b.i, acc.r));
+  acc.i = fma(a.r, b.i, fma(a.i, b.r, acc.i));
+}
+// acc += a * conj(b)
+template <typename T> __device__ __forceinline__ void cmacc(Cx<T>& acc, Cx<T> a, Cx<T> b) {
+  acc.r = fma(a.r, b.r, fma(a.i, b.i, acc.r));
+  acc.i = fma(a.i, b.r, fma(-a.r, b.i, acc.i));
+}
+// Re(conj(a) * b)
+template <typename T> __device__ __forceinline__ T cdot_re(Cx<T> a, Cx<T> b) { return a.r * b.r + a.i * b.i; }
+
+// 2x2 complex Jones matrix, row-major [00, 01, 10, 11].
+template <typename T>
+struct Jones {
+  Cx<T> a, b, c, d;
+};
+
+template <typename T> __device__ __forceinline__ Jones<T> jzero() {
+  Jones<T> z;
+  z.a = z.b = z.c = z.d = Cx<T>{T(0), T(0)};
+  return z;
+}
+template <typename T> __device__ __forceinline__ Jones<T> jadd(const Jones<T>& x, const Jones<T>& y) {
+  return {x.a + y.a, x.b + y.b, x.c + y.c, x.d + y.d};
+}
+template <typename T> __device__ __forceinline__ Jones<T> jscale(const Jones<T>& x, T s) {
+  return {x.a * s, x.b * s, x.c * s, x.d * s};
+}
+// X * Y
+template <typename T> __device__ __forceinline__ Jones<T> jmul(const Jones<T>& X, const Jones<T>& Y) {
+  Jones<T> R;
+  R.a = cmul(X.a, Y.a); cmac(R.a, X.b, Y.c);
+  R.b = cmul(X.a, Y.b); cmac(R.b, X.b, Y.d);
+  R.c = cmul(X.c, Y.a); cmac(R.c, X.d, Y.c);
+  R.d = cmul(X.c, Y.b); cmac(R.d, X.d, Y.d);
+  return R;
+}
+// X * Y^H
+template <typename T> __device__ __forceinline__ Jones<T> jmulh(const Jones<T>& X, const Jones<T>& Y) {
+  Jones<T> R;
+  R.a = cmulc(X.a, Y.a); cmacc(R.a, X.b, Y.b);
+  R.b = cmulc(X.a, Y.c); cmacc(R.b, X.b, Y.d);
+  R.c = cmulc(X.c, Y.a); cmacc(R.c, X.d, Y.b);
+  R.d = cmulc(X.c, Y.c); cmacc(R.d, X.d, Y.d);
+  return R;
+}
+// X^H * Y
+template <typename T> __device__ __forceinline__ Jones<T> jhmul(const Jones<T>& X, const Jones<T>& Y) {
+  Jones<T> R;
+  // (X^H)_{ij} = conj(X_{ji})
+  R.a = cmul(conj(X.a), Y.a); cmac(R.a, conj(X.c), Y.c);
+  R.b = cmul(conj(X.a), Y.b); cmac(R.b, conj(X.c), Y.d);
+  R.c = cmul(conj(X.b), Y.a); cmac(R.c, conj(X.d), Y.c);
+  R.d = cmul(conj(X.b), Y.b); cmac(R.d, conj(X.d), Y.d);
+  return R;
+}
+// acc += X * Y^H
+template <typename T> __device__ __forceinline__ void jmac_h(Jones<T>& acc, const Jones<T>& X, const Jones<T>& Y) {
+  cmacc(acc.a, X.a, Y.a); cmacc(acc.a, X.b, Y.b);
+  cmacc(acc.b, X.a, Y.c); cmacc(acc.b, X.b, Y.d);
+  cmacc(acc.c, X.c, Y.a); cmacc(acc.c, X.d, Y.b);
+  cmacc(acc.d, X.c, Y.c); cmacc(acc.d, X.d, Y.d);
+}
+// acc += X * Y
+template <typename T> __device__ __forceinline__ void jmac(Jones<T>& acc, const Jones<T>& X, const Jones<T>& Y) {
+  cmac(acc.a, X.a, Y.a); cmac(acc.a, X.b, Y.c);
+  cmac(acc.b, X.a, Y.b); cmac(acc.b, X.b, Y.d);
+  cmac(acc.c, X.c, Y.a); cmac(acc.c, X.d, Y.c);
+  cmac(acc.d, X.c, Y.b); cmac(acc.d, X.d, Y.d);
+}
+// X^H
+template <typename T> __device__ __forceinline__ Jones<T> jherm(const Jones<T>& X) {
+  return {conj(X.a), conj(X.c), conj(X.b), conj(X.d)};
+}
+// Re <X, Y> = Re sum_ij conj(X_ij) Y_ij
+template <typename T> __device__ __forceinline__ T jdot_re(const Jones<T>& X, const Jones<T>& Y) {
+  return cdot_re(X.a, Y.a) + cdot_re(X.b, Y.b) + cdot_re(X.c, Y.c) + cdot_re(X.d, Y.d);
+}
+
+// ---- loads / stores of interleaved complex Jones -------------------------
+template <typename T> __device__ __forceinline__ Jones<T> jload(const T* p);
+template <> __device__ __forceinline__ Jones<float> jload<float>(const float* p) {
+  float4 u = *reinterpret_cast<const float4*>(p);
+  float4 v = *reinterpret_cast<const float4*>(p + 4);
+  return {{u.x, u.y}, {u.z, u.w}, {v.x, v.y}, {v.z, v.w}};
+}
+template <> __device__ __forceinline__ Jones<double> jload<double>(const double* p) {
+  double2 u = *reinterpret_cast<const double2*>(p);
+  double2 v = *reinterpret_cast<const double2*>(p + 2);
+  double2 w = *reinterpret_cast<const double2*>(p + 4);
+  double2 x = *reinterpret_cast<const double2*>(p + 6);
+  return {{u.x, u.y}, {v.x, v.y}, {w.x, w.y}, {x.x, x.y}};
+}
+template <typename T> __device__ __forceinline__ Jones<T> jldg(const T* p);
+template <> __device__ __forceinline__ Jones<float> jldg<float>(const float* p) {
+  float4 u = __ldg(reinterpret_cast<const float4*>(p));
+  float4 v = __ldg(reinterpret_cast<const float4*>(p + 4));
+  return {{u.x, u.y}, {u.z, u.w}, {v.x, v.y}, {v.z, v.w}};
+}
+template <> __device__ __forceinline__ Jones<double> jldg<double>(const double* p) {
+  double2 u = __ldg(reinterpret_cast<const double2*>(p));
+  double2 v = __ldg(reinterpret_cast<const double2*>(p + 2));
+  double2 w = __ldg(reinterpret_cast<const double2*>(p + 4));
+  double2 x = __ldg(reinterpret_cast<const double2*>(p + 6));
+  return {{u.x, u.y}, {v.x, v.y}, {w.x, w.y}, {x.x, x.y}};
+}
+template <typename T> __device__ __forceinline__ void jstore(T* p, const Jones<T>& J);
+template <> __device__ __forceinline__ void jstore<float>(float* p, const Jones<float>& J) {
+  *reinterpret_cast<float4*>(p) = make_float4(J.a.r, J.a.i, J.b.r, J.b.i);
+  *reinterpret_cast<float4*>(p + 4) = make_float4(J.c.r, J.c.i, J.d.r, J.d.i);
+}
+template <> __device__ __forceinline__ void jstore<double>(double* p, const Jones<double>& J) {
+  *reinterpret_cast<double2*>(p) = make_double2(J.a.r, J.a.i);
+  *reinterpret_cast<double2*>(p + 2) = make_double2(J.b.r, J.b.i);
+  *reinterpret_cast<double2*>(p + 4) = make_double2(J.c.r, J.c.i);
+  *reinterpret_cast<double2*>(p + 6) = make_double2(J.d.r, J.d.i);
+}
+
+// ---- scalar helpers -------------------------------------------------------
+__device__ __forceinline__ float mb_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double mb_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float mb_exp(float x) { return expf(x); }
+__device__ __forceinline__ double mb_exp(double x) { return exp(x); }
+__device__ __forceinline__ float mb_pow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double mb_pow(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float mb_floor(float x) { return floorf(x); }
+__device__ __forceinline__ double mb_floor(double x) { return floor(x); }
+__device__ __forceinline__ float mb_log(float x) { return logf(x); }
+__device__ __forceinline__ double mb_log(double x) { return log(x); }
+template <typename T> __device__ __forceinline__ T mb_clamp(T x, T lo, T hi) { return x < lo ? lo : (x > hi ? hi : x); }
+template <typename T> __device__ __forceinline__ T cabs_(Cx<T> z) { return mb_sqrt(z.r * z.r + z.i * z.i); }
+
+// ---- brightness square root (a1) -----------------------------------------
+// B = [[I+Q, U+iV], [U-iV, I-Q]] * (nu/nu_ref)^alpha,
+// sqrt(B) = (B + s*1) / t with s = sqrt(det B), t = sqrt(tr B + 2 s); t := 1
+// when s == t == 0.  CPUSolver.py:235-317, brightness.cuh:108-164.
+// A determinant that rounds below zero is clamped to zero.
+template <typename T>
+__device__ __forceinline__ Jones<T> brightness_sqrt(T I, T Q, T U, T V, T power) {
+  T b0 = (I + Q) * power, b3 = (I - Q) * power;
+  T ur = U * power, vi = V * power;
+  T trace = b0 + b3;
+  T det = b0 * b3 - (ur * ur + vi * vi);
+  det = det < T(0) ? T(0) : det;
+  T s = mb_sqrt(det);
+  T t = mb_sqrt(trace + T(2) * s);
+  if (s == T(0) && t == T(0)) t = T(1);
+  T rt = T(1) / t;
+  Jones<T> R;
+  R.a = {(b0 + s) * rt, T(0)};
+  R.b = {ur * rt, vi * rt};
+  R.c = {ur * rt, -vi * rt};
+  R.d = {(b3 + s) * rt, T(0)};
+  return R;
+}
+
+// ---- phase (a2) ----------------------------------------------------------
+// K = exp(-2 pi i phi nu / c), phi = u l + v m + w (n - 1).  The phase
+// argument and its range reduction are always evaluated in FP64
+// (CPUSolver.py:162-195).
+template <typename T> __device__ __forceinline__ Cx<T> phase_from_phi(double phi, double freq);
+// FP64: exp(i * ((-2 pi phi) nu) / c), in the oracle's evaluation order.
+template <> __device__ __forceinline__ Cx<double> phase_from_phi<double>(double phi, double freq) {
+  double arg = ((-2.0 * kPi) * phi * freq) / kLightSpeed;
+  double s, c;
+  sincos(arg, &s, &c);
+  return {c, s};
+}
+// FP32: cycles = phi nu / c and its fractional part in FP64, then an FP32
+// sincospi of the reduced argument.
+template <> __device__ __forceinline__ Cx<float> phase_from_phi<float>(double phi, double freq) {
+  double cycles = phi * freq / kLightSpeed;
+  double frac = cycles - rint(cycles);
+  float s, c;
+  sincospif(-2.0f * static_cast<float>(frac), &s, &c);
+  return {c, s};
+}
+
+// Same, with nu / c precomputed per channel (fused kernels).
+template <typename T> __device__ __forceinline__ Cx<T> phase_from_cycles(double phi, double nu_over_c);
+template <> __device__ __forceinline__ Cx<double> phase_from_cycles<double>(double phi, double nu_over_c) {
+  double cycles = phi * nu_over_c;
+  double frac = cycles - rint(cycles);
+  double s, c;
+  sincospi(-2.0 * frac, &s, &c);
+  return {c, s};
+}
+template <> __device__ __forceinline__ Cx<float> phase_from_cycles<float>(double phi, double nu_over_c) {
+  double cycles = phi * nu_over_c;
+  double frac = cycles - rint(cycles);
+  float s, c;
+  sincospif(-2.0f * static_cast<float>(frac), &s, &c);
+  return {c, s};
+}
+
+// ---- beam cube (a3) ------------------------------------------------------
+// Beam grid position along one axis: scale * (x - lower), clamped to
+// [0, n-1], split into the lower grid index, the upper grid index and the
+// offset.  CPUSolver.py:394-414 (the oracle form ((n-1)(x-lo))/(hi-lo) is
+// used in FP64, the pre-scaled form in FP32).
+template <typename T>
+struct GridPos {
+  int i0, i1;
+  T d;
+  bool inside;  // strictly inside (0, n-1): derivative w.r.t. x is non-zero
+};
+
+template <typename T>
+__device__ __forceinline__ GridPos<T> grid_pos(T x, T lower, T upper, T scale, int n) {
+  T v;
+  if (sizeof(T) == 8) v = (T(n - 1) * (x - lower)) / (upper - lower);
+  else v = scale * (x - lower);
+  GridPos<T> g;
+  g.inside = (v > T(0)) && (v < T(n - 1));
+  v = mb_clamp(v, T(0), T(n - 1));
+  T f0 = mb_floor(v);
+  g.i0 = static_cast<int>(f0);
+  g.i1 = min(g.i0 + 1, n - 1);
+  g.d = v - f0;
+  return g;
+}
+
+// Channel grid of the beam cube for one frequency.
+template <typename T>
+struct ChanPos {
+  int c0, c1;
+  T d;
+};
+
+template <typename T>
+__device__ __forceinline__ ChanPos<T> chan_pos(T freq, T lfreq, T ufreq, int nud) {
+  T v = (T(nud - 1) * (freq - lfreq)) / (ufreq - lfreq);
+  v = mb_clamp(v, T(0), T(nud - 1));
+  T f0 = mb_floor(v);
+  ChanPos<T> c;
+  c.c0 = static_cast<int>(f0);
+  c.c1 = min(c.c0 + 1, nud - 1);
+  c.d = v - f0;
+  return c;
+}
+
+struct BeamGeom {
+  int lw, mh, nud;
+};
+
+// Weighted gather of the 4 correlations of one beam-cube corner.
+template <typename T>
+__device__ __forceinline__ void beam_corner(const T* __restrict__ E_beam, const BeamGeom& G,
+                                            int il, int im, int ic, T w, Jones<T>& sum, T (&amp)[4]) {
+  const T* p = E_beam + 8 * ((static_cast<size_t>(il) * G.mh + im) * G.nud + ic);
+  Jones<T> e = jldg<T>(p);
+  sum.a = sum.a + e.a * w; amp[0] += w * cabs_(e.a);
+  sum.b = sum.b + e.b * w; amp[1] += w * cabs_(e.b);
+  sum.c = sum.c + e.c * w; amp[2] += w * cabs_(e.c);
+  sum.d = sum.d + e.d * w; amp[3] += w * cabs_(e.d);
+}
+
+template <typename T>
+__device__ __forceinline__ Cx<T> renorm(Cx<T> z, T amp) {
+  T r = cabs_(z);
+  T norm = T(1) / r;
+  if (!isfinite(norm)) norm = T(1);
+  return z * (norm * amp);
+}
+
+// Trilinear, amplitude-renormalised beam value at grid positions gl, gm
+// and channel position ch (CPUSolver.py:416-475, RimeEBeam.py:94-116,
+// 287-339).  Corner order and weights follow the oracle.
+template <typename T>
+__device__ __forceinline__ Jones<T> beam_interp(const T* __restrict__ E_beam, const BeamGeom& G,
+                                                const GridPos<T>& gl, const GridPos<T>& gm,
+                                                const ChanPos<T>& ch) {
+  Jones<T> sum = jzero<T>();
+  T amp[4] = {T(0), T(0), T(0), T(0)};
+  T ld = gl.d, md = gm.d, cd = ch.d;
+  beam_corner(E_beam, G, gl.i0, gm.i0, ch.c0, (T(1) - ld) * (T(1) - md) * (T(1) - cd), sum, amp);
+  beam_corner(E_beam, G, gl.i1, gm.i0, ch.c0, ld * (T(1) - md) * (T(1) - cd), sum, amp);
+  beam_corner(E_beam, G, gl.i0, gm.i1, ch.c0, (T(1) - ld) * md * (T(1) - cd), sum, amp);
+  beam_corner(E_beam, G, gl.i1, gm.i1, ch.c0, ld * md * (T(1) - cd), sum, amp);
+  beam_corner(E_beam, G, gl.i0, gm.i0, ch.c1, (T(1) - ld) * (T(1) - md) * cd, sum, amp);
+  beam_corner(E_beam, G, gl.i1, gm.i0, ch.c1, ld * (T(1) - md) * cd, sum, amp);
+  beam_corner(E_beam, G, gl.i0, gm.i1, ch.c1, (T(1) - ld) * md * cd, sum, amp);
+  beam_corner(E_beam, G, gl.i1, gm.i1, ch.c1, ld * md * cd, sum, amp);
+  Jones<T> E;
+  E.a = renorm(sum.a, amp[0]);
+  E.b = renorm(sum.b, amp[1]);
+  E.c = renorm(sum.c, amp[2]);
+  E.d = renorm(sum.d, amp[3]);
+  return E;
+}
+
+// Rotate (l, m) by the parallactic angle, add the pointing error and scale
+// by the antenna scaling (CPUSolver.py:367-390).
+template <typename T>
+__device__ __forceinline__ void beam_lm(T l0, T m0, T sin_pa, T cos_pa, T pe_l, T pe_m, T sc_l, T sc_m,
+                                        T& l, T& m) {
+  l = (l0 * cos_pa - m0 * sin_pa + pe_l) * sc_l;
+  m = (l0 * sin_pa + m0 * cos_pa + pe_m) * sc_m;
+}
+
+// ---- source shapes (a5) --------------------------------------------------
+// Gaussian: exp(-((u1 k R)^2 + (v1 k)^2)), u1 = u em - v el, v1 = u el + v em,
+// k = gauss_scale * nu (CPUSolver.py:59-103).
+template <typename T>
+__device__ __forceinline__ T gauss_shape(T u, T v, T el, T em, T R, T k) {
+  T u1 = (u * em - v * el) * k * R;
+  T v1 = (u * el + v * em) * k;
+  return mb_exp(-(u1 * u1 + v1 * v1));
+}
+// Sersic: 1 / (d sqrt d), d = 1 + (u1 k S)^2 + (v1 k S)^2, u1 = u(1+e1) + v e2,
+// v1 = u e2 + v(1-e1), S = R / (1 - e1^2 - e2^2), k = 2 pi nu / c
+// (CPUSolver.py:105-160).
+template <typename T>
+__device__ __forceinline__ T sersic_shape(T u, T v, T e1, T e2, T R, T k) {
+  T S = R / (T(1) - e1 * e1 - e2 * e2);
+  T u1 = (u * (T(1) + e1) + v * e2) * k * S;
+  T v1 = (u * e2 + v * (T(1) - e1)) * k * S;
+  T d = T(1) + u1 * u1 + v1 * v1;
+  return T(1) / (d * mb_sqrt(d));
+}
+
+// Source type of global source index s (point, gaussian, sersic order,
+// montblanc/src_types.py:40-44).
+enum SrcType { SRC_POINT = 0, SRC_GAUSS = 1, SRC_SERSIC = 2 };
+
+// Index of unordered antenna pair (p <= q) in the packed upper triangle.
+__host__ __device__ __forceinline__ int pair_index(int p, int q, int na) {
+  return p * na - (p * (p - 1)) / 2 + (q - p);
+}
+
+}  // namespace mb

@@ -1,0 +1,920 @@
+// Fused RIME v4 forward chi^2 and adjoint, CUDA-core arithmetic.
+//
+// One CTA owns one (time, channel) unit.  For every tile of sources it
+//   1. forms the per-antenna terms J(s, a) = E(s, a) . K(s, a) . sqrt(B)(s)
+//      in shared memory (the "producer"; nothing is written to HBM),
+//   2. accumulates the coherencies of all antenna pairs p <= q,
+//      V_pq += shape * J_p J_q^H, from register tiles of RP x RQ antennas,
+// and finally applies G, flags, weights and the residual per baseline and
+// reduces chi^2 (the epilogue), optionally leaving d chi^2 / dV and
+// d chi^2 / dG in the workspace for the adjoint.
+//
+// The adjoint CTA, per (time, channel), rebuilds the Hermitian matrix of
+// d chi^2 / dV over antenna pairs, recomputes J per source tile, forms
+// d chi^2 / dJ_a = sum_b shape_ab Y_ab J_b, then chains through E (beam
+// interpolation), K (phase) and sqrt(B) (brightness) to the source
+// parameters, reducing over antennas in shared memory and over time and
+// channel with FP64 atomics.
+//
+// Reference behaviour: CPUSolver.py:59-737 (forward maths),
+// RimeSumCoherencies.py:103-393 (epilogue, source-batch semantics).  The
+// adjoint has no reference counterpart.
+#include <algorithm>
+
+#include "mb_fused.h"
+
+namespace mb {
+
+__global__ void sum_partials_kernel(const double* __restrict__ partial, int n, double scale,
+                                    double* __restrict__ out);
+mb_status tc_point_coherencies(const FusedArgs<float>& A, mb_mode mode, float* Vpoint, cudaStream_t stream);
+size_t tc_scratch_bytes(const mb_dims* d);
+
+namespace {
+
+template <typename T> struct FwdTile;
+template <> struct FwdTile<float> { static constexpr int RP = 2, RQ = 4, ST = 16; };
+template <> struct FwdTile<double> { static constexpr int RP = 1, RQ = 2, ST = 8; };
+template <typename T> struct AdjTile;
+template <> struct AdjTile<float> { static constexpr int RA = 2, RS = 4, ST = 16; };
+template <> struct AdjTile<double> { static constexpr int RA = 1, RS = 2, ST = 8; };
+
+constexpr int kNAcc = 10;  // l, m, I, Q, U, V, alpha, shape0, shape1, shape2
+
+int count_pair_tiles(int na, int RP, int RQ) {
+  int npt = (na + RP - 1) / RP, nqt = (na + RQ - 1) / RQ, n = 0;
+  for (int ip = 0; ip < npt; ++ip) n += nqt - (ip * RP) / RQ;
+  return n;
+}
+
+template <typename T>
+SmemPlan make_plan(int na, bool adjoint) {
+  SmemPlan S;
+  S.nap = (na + 3) / 4 * 4;
+  S.st = adjoint ? AdjTile<T>::ST : FwdTile<T>::ST;
+  S.npairs = na * (na + 1) / 2;
+  S.nitems = count_pair_tiles(na, FwdTile<T>::RP, FwdTile<T>::RQ);
+  size_t o = 0;
+  auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 16); return r; };
+  S.off_ant = take(sizeof(AntInfo<T>) * na);
+  S.off_antd = take(sizeof(double) * 3 * na);
+  S.off_src = take(sizeof(SrcInfo<T>) * S.st);
+  S.off_J = take(sizeof(Jones<T>) * S.st * S.nap);
+  S.off_gJ = take(adjoint ? sizeof(Jones<T>) * S.st * S.nap : 0);
+  S.off_V = take(sizeof(Jones<T>) * S.npairs);
+  S.off_items = take(adjoint ? 0 : sizeof(int) * (S.nitems + 128));
+  S.off_acc = take(adjoint ? sizeof(T) * S.st * kNAcc : 0);
+  S.off_red = take(sizeof(double) * 32);
+  S.total = o;
+  return S;
+}
+
+// ---------------------------------------------------------------------------
+// Shared set-up and producer
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ void load_antennas(const FusedArgs<T>& A, int t, int ch, AntInfo<T>* sa, double* sad) {
+  for (int a = threadIdx.x; a < A.na; a += blockDim.x) {
+    size_t ta = size_t(t) * A.lna + a;
+    AntInfo<T> ai;
+    if (sizeof(T) == 8) {
+      double s_, c_; sincos(double(A.pa[ta]), &s_, &c_); ai.sin_pa = T(s_); ai.cos_pa = T(c_);
+    } else {
+      float s_, c_; sincosf(float(A.pa[ta]), &s_, &c_); ai.sin_pa = T(s_); ai.cos_pa = T(c_);
+    }
+    size_t tac = ta * A.lchan + ch;
+    ai.pe_l = A.pe[2 * tac]; ai.pe_m = A.pe[2 * tac + 1];
+    size_t ac = size_t(a) * A.lchan + ch;
+    ai.sc_l = A.sc[2 * ac]; ai.sc_m = A.sc[2 * ac + 1];
+    ai.u = A.uvw[3 * ta]; ai.v = A.uvw[3 * ta + 1];
+    sa[a] = ai;
+    if (sad) { sad[3 * a] = A.uvw[3 * ta]; sad[3 * a + 1] = A.uvw[3 * ta + 1]; sad[3 * a + 2] = A.uvw[3 * ta + 2]; }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ int src_type(const FusedArgs<T>& A, int s) {
+  return s < A.npsrc ? SRC_POINT : (s < A.npsrc + A.ngsrc ? SRC_GAUSS : SRC_SERSIC);
+}
+
+// Per-source information of the tile [s0, s0 + ns) at time t, frequency f.
+template <typename T>
+__device__ void load_sources(const FusedArgs<T>& A, int t, int ch, int s0, int ns, SrcInfo<T>* ss) {
+  T f = A.freq[ch], rf = A.ref_freq[ch];
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) {
+    int s = s0 + i;
+    SrcInfo<T> si;
+    si.l = A.lm[2 * s]; si.m = A.lm[2 * s + 1];
+    size_t st = size_t(s) * A.ltime + t;
+    si.I = A.stokes[4 * st]; si.Q = A.stokes[4 * st + 1];
+    si.U = A.stokes[4 * st + 2]; si.V = A.stokes[4 * st + 3];
+    si.power = mb_pow(f / rf, A.alpha[st]);
+    si.B = brightness_sqrt<T>(si.I, si.Q, si.U, si.V, si.power);
+    si.type = src_type(A, s);
+    si.s0 = si.s1 = si.s2 = T(0);
+    if (si.type == SRC_GAUSS) {
+      int g = s - A.npsrc;
+      si.s0 = A.gauss[g]; si.s1 = A.gauss[A.lgsrc + g]; si.s2 = A.gauss[2 * A.lgsrc + g];
+    } else if (si.type == SRC_SERSIC) {
+      int x = s - A.npsrc - A.ngsrc;
+      si.s0 = A.sersic[x]; si.s1 = A.sersic[A.lssrc + x]; si.s2 = A.sersic[2 * A.lssrc + x];
+    }
+    ss[i] = si;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ Cx<T> phase_term(const FusedArgs<T>& A, int t, int s, int a, T f, double nu_over_c) {
+  double phi = A.phi[(size_t(t) * A.nsrc + s) * A.na + a];
+  if (sizeof(T) == 8) return phase_from_phi<T>(phi, double(f));
+  return phase_from_cycles<T>(phi, nu_over_c);
+}
+
+// J(s, a) for the tile into sJ[si * nap + a]; padded antennas get zeros.
+template <typename T>
+__device__ void produce_jones(const FusedArgs<T>& A, const SmemPlan& S, int t, int ch, int s0, int ns,
+                              const SrcInfo<T>* ss, const AntInfo<T>* sa, Jones<T>* sJ, const ChanPos<T>& cp) {
+  const T f = A.freq[ch];
+  const double nu_over_c = double(f) / kLightSpeed;
+  const BeamGeom G{A.lw, A.mh, A.nud};
+  for (int i = threadIdx.x; i < ns * S.nap; i += blockDim.x) {
+    int si = i / S.nap, a = i - si * S.nap;
+    Jones<T> J = jzero<T>();
+    if (a < A.na) {
+      const SrcInfo<T>& src = ss[si];
+      Cx<T> K = phase_term(A, t, s0 + si, a, f, nu_over_c);
+      const AntInfo<T>& ai = sa[a];
+      T l, m;
+      beam_lm<T>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
+      GridPos<T> gl = grid_pos<T>(l, A.ll, A.ul, A.lscale, A.lw);
+      GridPos<T> gm = grid_pos<T>(m, A.lmm, A.um, A.mscale, A.mh);
+      Jones<T> E = beam_interp<T>(A.E_beam, G, gl, gm, cp);
+      Jones<T> KB = {cmul(K, src.B.a), cmul(K, src.B.b), cmul(K, src.B.c), cmul(K, src.B.d)};
+      J = jmul(E, KB);
+    }
+    sJ[i] = J;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T shape_factor(int type, T u, T v, T s0, T s1, T s2, T kg, T ks) {
+  return type == SRC_GAUSS ? gauss_shape<T>(u, v, s0, s1, s2, kg) : sersic_shape<T>(u, v, s0, s1, s2, ks);
+}
+
+template <typename T>
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ void atomic_add_jones(Jones<T>* dst, const Jones<T>& x) {
+  T* d = reinterpret_cast<T*>(dst);
+  atomicAdd(d + 0, x.a.r); atomicAdd(d + 1, x.a.i); atomicAdd(d + 2, x.b.r); atomicAdd(d + 3, x.b.i);
+  atomicAdd(d + 4, x.c.r); atomicAdd(d + 5, x.c.i); atomicAdd(d + 6, x.d.r); atomicAdd(d + 7, x.d.i);
+}
+
+// ---------------------------------------------------------------------------
+// Epilogue (shared with the tensor-core path)
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const Jones<T>* sV, Jones<T>* scratch,
+                         double* red) {
+  Jones<T>* sG = scratch;
+  Jones<T>* sdG = scratch + A.na;
+  for (int a = threadIdx.x; a < A.na; a += blockDim.x) {
+    sG[a] = jldg<T>(A.G + 8 * ((size_t(t) * A.lna + a) * A.lchan + ch));
+    if (A.want_grad) sdG[a] = jzero<T>();
+  }
+  __syncthreads();
+  double part = 0.0;
+  for (int bl = threadIdx.x; bl < A.nbl; bl += blockDim.x) {
+    size_t tbl = size_t(t) * A.lnbl + bl;
+    int p = A.ant1[tbl], q = A.ant2[tbl];
+    Jones<T> V = p <= q ? sV[pair_index(p, q, A.na)] : jherm(sV[pair_index(q, p, A.na)]);
+    size_t vidx = tbl * A.lchan + ch;
+    if (A.accumulate_in) V = jadd(V, jload<T>(A.model_vis + 8 * vidx));
+    if (A.partial_out) {
+      jstore(A.model_vis + 8 * vidx, V);
+      continue;
+    }
+    const Jones<T> Gp = sG[p], Gq = sG[q];
+    Jones<T> M = jmulh(jmul(Gp, V), Gq);
+    Jones<T> O = jldg<T>(A.obs + 8 * vidx);
+    uchar4 fl = *reinterpret_cast<const uchar4*>(A.flag + 4 * vidx);
+    const uint8_t fv[4] = {fl.x, fl.y, fl.z, fl.w};
+    T w4[4] = {T(1), T(1), T(1), T(1)};
+    if (A.weights) {
+      for (int k = 0; k < 4; ++k) w4[k] = A.weight[4 * vidx + k];
+    }
+    Cx<T>* m4 = &M.a;
+    Cx<T>* o4 = &O.a;
+    Jones<T> R, gM;
+    Cx<T>* r4 = &R.a;
+    Cx<T>* g4 = &gM.a;
+    T term = T(0);
+    const T gscale = A.weights ? T(-2) : T(-2.0 * A.inv_sigma2);
+    for (int k = 0; k < 4; ++k) {
+      if (fv[k] > 0) { m4[k] = Cx<T>{T(0), T(0)}; o4[k] = Cx<T>{T(0), T(0)}; }
+      r4[k] = o4[k] - m4[k];
+      T re2 = r4[k].r * r4[k].r, im2 = r4[k].i * r4[k].i;
+      if (A.weights) { re2 *= w4[k]; im2 *= w4[k]; }
+      term += re2 + im2;
+      g4[k] = fv[k] > 0 ? Cx<T>{T(0), T(0)} : r4[k] * (gscale * w4[k]);
+    }
+    if (A.model_vis) jstore(A.model_vis + 8 * vidx, A.residuals ? R : M);
+    if (A.chi2) A.chi2[vidx] = term;
+    part += double(term);
+    if (A.want_grad) {
+      Jones<T> gV = jmul(jhmul(Gp, gM), Gq);
+      jstore(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch), gV);
+      atomic_add_jones(&sdG[p], jmul(gM, jmulh(Gq, V)));
+      atomic_add_jones(&sdG[q], jmul(jherm(gM), jmul(Gp, V)));
+    }
+  }
+  double tot = block_sum<T>(part, red);
+  if (threadIdx.x == 0) A.partial[unit] = tot;
+  if (A.want_grad) {
+    __syncthreads();
+    for (int a = threadIdx.x; a < A.na; a += blockDim.x)
+      jstore(A.dG + 8 * ((size_t(t) * A.na + a) * A.nchan + ch), sdG[a]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Forward
+// ---------------------------------------------------------------------------
+template <typename T, int RP, int RQ>
+__device__ void consume_pairs(const FusedArgs<T>& A, const SmemPlan& S, int ns, const SrcInfo<T>* ss,
+                              const AntInfo<T>* sa, const Jones<T>* sJ, Jones<T>* sV, const int* items,
+                              bool extended, T kg, T ks) {
+  for (int k = threadIdx.x; k < S.nitems; k += blockDim.x) {
+    int it = items[k];
+    int p0 = (it & 0xffff) * RP, q0 = (it >> 16) * RQ;
+    Jones<T> acc[RP][RQ];
+    T u[RP][RQ], v[RP][RQ];
+#pragma unroll
+    for (int r = 0; r < RP; ++r)
+#pragma unroll
+      for (int c = 0; c < RQ; ++c) {
+        int p = p0 + r, q = q0 + c;
+        bool ok = p <= q && q < A.na;
+        acc[r][c] = ok ? sV[pair_index(p, q, A.na)] : jzero<T>();
+        if (extended) {
+          int pp = min(p, A.na - 1), qq = min(q, A.na - 1);
+          u[r][c] = sa[qq].u - sa[pp].u;
+          v[r][c] = sa[qq].v - sa[pp].v;
+        }
+      }
+    for (int si = 0; si < ns; ++si) {
+      Jones<T> Ja[RP], Jb[RQ];
+#pragma unroll
+      for (int r = 0; r < RP; ++r) Ja[r] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + p0 + r));
+#pragma unroll
+      for (int c = 0; c < RQ; ++c) Jb[c] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + q0 + c));
+      if (!extended) {
+#pragma unroll
+        for (int r = 0; r < RP; ++r)
+#pragma unroll
+          for (int c = 0; c < RQ; ++c) jmac_h(acc[r][c], Ja[r], Jb[c]);
+      } else {
+        const SrcInfo<T>& src = ss[si];
+#pragma unroll
+        for (int r = 0; r < RP; ++r)
+#pragma unroll
+          for (int c = 0; c < RQ; ++c) {
+            T sh = shape_factor<T>(src.type, u[r][c], v[r][c], src.s0, src.s1, src.s2, kg, ks);
+            jmac_h(acc[r][c], jscale(Ja[r], sh), Jb[c]);
+          }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RP; ++r)
+#pragma unroll
+      for (int c = 0; c < RQ; ++c) {
+        int p = p0 + r, q = q0 + c;
+        if (p <= q && q < A.na) sV[pair_index(p, q, A.na)] = acc[r][c];
+      }
+  }
+}
+
+template <typename T, int RP, int RQ>
+__global__ void __launch_bounds__(kFusedThreads) coh_fwd_kernel(FusedArgs<T> A, SmemPlan S) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  AntInfo<T>* sa = reinterpret_cast<AntInfo<T>*>(smem + S.off_ant);
+  SrcInfo<T>* ss = reinterpret_cast<SrcInfo<T>*>(smem + S.off_src);
+  Jones<T>* sJ = reinterpret_cast<Jones<T>*>(smem + S.off_J);
+  Jones<T>* sV = reinterpret_cast<Jones<T>*>(smem + S.off_V);
+  int* items = reinterpret_cast<int*>(smem + S.off_items);
+  double* red = reinterpret_cast<double*>(smem + S.off_red);
+
+  const int unit = blockIdx.x;
+  const int t = unit / A.nchan, ch = unit - t * A.nchan;
+  load_antennas(A, t, ch, sa, nullptr);
+  const bool have_point_tc = A.Vpoint != nullptr;
+  for (int i = threadIdx.x; i < S.npairs; i += blockDim.x) {
+    Jones<T> z = jzero<T>();
+    if (have_point_tc) {
+      // Point-source coherencies from the tensor-core kernel: packed
+      // (p, q) -> 4 complex, row-major over the full na x na matrix.
+      int p = 0, rem = i;
+      while (rem >= A.na - p) { rem -= A.na - p; ++p; }
+      int q = p + rem;
+      const float* src = A.Vpoint + (size_t(unit) * A.na * A.na + size_t(p) * A.na + q) * 8;
+      z.a = {T(src[0]), T(src[1])}; z.b = {T(src[2]), T(src[3])};
+      z.c = {T(src[4]), T(src[5])}; z.d = {T(src[6]), T(src[7])};
+    }
+    sV[i] = z;
+  }
+  if (threadIdx.x == 0) {
+    const int npt = (A.na + RP - 1) / RP, nqt = (A.na + RQ - 1) / RQ;
+    int k = 0;
+    for (int ip = 0; ip < npt; ++ip)
+      for (int jq = (ip * RP) / RQ; jq < nqt; ++jq) items[k++] = ip | (jq << 16);
+  }
+  __syncthreads();
+
+  const T f = A.freq[ch];
+  const ChanPos<T> cp = chan_pos<T>(f, A.lfreq, A.ufreq, A.nud);
+  const T kg = A.gauss_scale * f, ks = A.two_pi_over_c * f;
+  const int sbeg = have_point_tc ? A.npsrc : 0;
+  for (int s0 = sbeg; s0 < A.nsrc;) {
+    int s1 = s0 < A.npsrc ? min(s0 + S.st, A.npsrc) : min(s0 + S.st, A.nsrc);
+    int ns = s1 - s0;
+    load_sources(A, t, ch, s0, ns, ss);
+    __syncthreads();
+    produce_jones(A, S, t, ch, s0, ns, ss, sa, sJ, cp);
+    __syncthreads();
+    consume_pairs<T, RP, RQ>(A, S, ns, ss, sa, sJ, sV, items, s0 >= A.npsrc, kg, ks);
+    __syncthreads();
+    s0 = s1;
+  }
+  epilogue(A, t, ch, unit, sV, sJ, red);
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint
+// ---------------------------------------------------------------------------
+// Y_ab: the Hermitian completion of the pair matrix X (see file header).
+template <typename T>
+__device__ __forceinline__ Jones<T> y_entry(const Jones<T>* sX, int a, int b, int na) {
+  if (a < b) return sX[pair_index(a, b, na)];
+  if (a > b) return jherm(sX[pair_index(b, a, na)]);
+  Jones<T> x = sX[pair_index(a, a, na)];
+  return jadd(x, jherm(x));
+}
+
+// Beam value and its derivatives with respect to the l and m grid offsets.
+template <typename T>
+__device__ void beam_interp_d(const T* __restrict__ E_beam, const BeamGeom& G, const GridPos<T>& gl,
+                              const GridPos<T>& gm, const ChanPos<T>& cp, Jones<T>& E, Jones<T>& dEl,
+                              Jones<T>& dEm) {
+  Jones<T> sum = jzero<T>(), dsl = jzero<T>(), dsm = jzero<T>();
+  T amp[4] = {0, 0, 0, 0}, dal[4] = {0, 0, 0, 0}, dam[4] = {0, 0, 0, 0};
+  const T ld = gl.d, md = gm.d, cd = cp.d;
+#pragma unroll
+  for (int corner = 0; corner < 8; ++corner) {
+    const bool hl = corner & 1, hm = corner & 2, hc = corner & 4;
+    const int il = hl ? gl.i1 : gl.i0, im = hm ? gm.i1 : gm.i0, ic = hc ? cp.c1 : cp.c0;
+    const T fl = hl ? ld : T(1) - ld, fm = hm ? md : T(1) - md, fc = hc ? cd : T(1) - cd;
+    const T w = fl * fm * fc, wl = (hl ? T(1) : T(-1)) * fm * fc, wm = fl * (hm ? T(1) : T(-1)) * fc;
+    const T* p = E_beam + 8 * ((size_t(il) * G.mh + im) * G.nud + ic);
+    Jones<T> e = jldg<T>(p);
+    const Cx<T>* e4 = &e.a;
+    Cx<T>* s4 = &sum.a; Cx<T>* l4 = &dsl.a; Cx<T>* m4 = &dsm.a;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      T ab = cabs_(e4[k]);
+      s4[k] = s4[k] + e4[k] * w; amp[k] += w * ab;
+      l4[k] = l4[k] + e4[k] * wl; dal[k] += wl * ab;
+      m4[k] = m4[k] + e4[k] * wm; dam[k] += wm * ab;
+    }
+  }
+  Cx<T>* E4 = &E.a; Cx<T>* dl4 = &dEl.a; Cx<T>* dm4 = &dEm.a;
+  const Cx<T>* s4 = &sum.a; const Cx<T>* l4 = &dsl.a; const Cx<T>* m4 = &dsm.a;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    T r = cabs_(s4[k]);
+    T inv = T(1) / r;
+    if (isfinite(inv)) {
+      E4[k] = s4[k] * (amp[k] * inv);
+      T drl = cdot_re(s4[k], l4[k]) * inv, drm = cdot_re(s4[k], m4[k]) * inv;
+      dl4[k] = (l4[k] * amp[k] + s4[k] * dal[k]) * inv - s4[k] * (amp[k] * drl * inv * inv);
+      dm4[k] = (m4[k] * amp[k] + s4[k] * dam[k]) * inv - s4[k] * (amp[k] * drm * inv * inv);
+    } else {
+      E4[k] = s4[k] * amp[k];
+      dl4[k] = l4[k] * amp[k] + s4[k] * dal[k];
+      dm4[k] = m4[k] * amp[k] + s4[k] * dam[k];
+    }
+  }
+}
+
+// Shape factor and its derivatives with respect to the 3 shape parameters.
+template <typename T>
+__device__ __forceinline__ T shape_and_grad(int type, T u, T v, T p0, T p1, T p2, T kg, T ks, T (&d)[3]) {
+  if (type == SRC_GAUSS) {
+    const T el = p0, em = p1, R = p2;
+    T a1 = u * em - v * el;
+    T u1 = a1 * kg * R, v1 = (u * el + v * em) * kg;
+    T c = mb_exp(-(u1 * u1 + v1 * v1));
+    d[0] = T(-2) * c * (u1 * (-v * kg * R) + v1 * (u * kg));
+    d[1] = T(-2) * c * (u1 * (u * kg * R) + v1 * (v * kg));
+    d[2] = T(-2) * c * (u1 * a1 * kg);
+    return c;
+  }
+  const T e1 = p0, e2 = p1, R = p2;
+  T den = T(1) - e1 * e1 - e2 * e2;
+  T Sc = R / den;
+  T a1 = u * (T(1) + e1) + v * e2, b1 = u * e2 + v * (T(1) - e1);
+  T u1 = a1 * ks * Sc, v1 = b1 * ks * Sc;
+  T dd = T(1) + u1 * u1 + v1 * v1;
+  T c = T(1) / (dd * mb_sqrt(dd));
+  T dS1 = Sc * T(2) * e1 / den, dS2 = Sc * T(2) * e2 / den;
+  T du_e1 = ks * (u * Sc + a1 * dS1), dv_e1 = ks * (-v * Sc + b1 * dS1);
+  T du_e2 = ks * (v * Sc + a1 * dS2), dv_e2 = ks * (u * Sc + b1 * dS2);
+  T du_R = a1 * ks / den, dv_R = b1 * ks / den;
+  T k3 = T(-3) * c / dd;
+  d[0] = k3 * (u1 * du_e1 + v1 * dv_e1);
+  d[1] = k3 * (u1 * du_e2 + v1 * dv_e2);
+  d[2] = k3 * (u1 * du_R + v1 * dv_R);
+  return c;
+}
+
+template <typename T, int RA, int RS>
+__device__ void adj_consume_point(const FusedArgs<T>& A, const SmemPlan& S, int ns, const Jones<T>* sJ,
+                                  const Jones<T>* sX, Jones<T>* sgJ) {
+  const int nat = S.nap / RA, nsg = (ns + RS - 1) / RS;
+  for (int k = threadIdx.x; k < nat * nsg; k += blockDim.x) {
+    const int sg = k / nat, at = k - sg * nat;
+    const int a0 = at * RA, sbase = sg * RS;
+    Jones<T> acc[RA][RS];
+#pragma unroll
+    for (int r = 0; r < RA; ++r)
+#pragma unroll
+      for (int c = 0; c < RS; ++c) acc[r][c] = jzero<T>();
+    for (int b = 0; b < A.na; ++b) {
+      Jones<T> Y[RA], Jb[RS];
+#pragma unroll
+      for (int r = 0; r < RA; ++r) Y[r] = (a0 + r < A.na) ? y_entry(sX, a0 + r, b, A.na) : jzero<T>();
+#pragma unroll
+      for (int c = 0; c < RS; ++c) {
+        int si = min(sbase + c, ns - 1);
+        Jb[c] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + b));
+      }
+#pragma unroll
+      for (int r = 0; r < RA; ++r)
+#pragma unroll
+        for (int c = 0; c < RS; ++c) jmac(acc[r][c], Y[r], Jb[c]);
+    }
+#pragma unroll
+    for (int r = 0; r < RA; ++r)
+#pragma unroll
+      for (int c = 0; c < RS; ++c)
+        if (sbase + c < ns) sgJ[(sbase + c) * S.nap + a0 + r] = acc[r][c];
+  }
+}
+
+template <typename T>
+__device__ void adj_consume_ext(const FusedArgs<T>& A, const SmemPlan& S, int ns, const SrcInfo<T>* ss,
+                                const AntInfo<T>* sa, const Jones<T>* sJ, const Jones<T>* sX, Jones<T>* sgJ,
+                                T* sacc, T kg, T ks) {
+  for (int k = threadIdx.x; k < ns * A.na; k += blockDim.x) {
+    const int si = k / A.na, a = k - si * A.na;
+    const SrcInfo<T>& src = ss[si];
+    const Jones<T> Ja = sJ[si * S.nap + a];
+    Jones<T> acc = jzero<T>();
+    T g0 = 0, g1 = 0, g2 = 0;
+    for (int b = 0; b < A.na; ++b) {
+      Jones<T> Y = y_entry(sX, a, b, A.na);
+      Jones<T> P = jmul(Y, sJ[si * S.nap + b]);
+      T d[3];
+      T c = shape_and_grad<T>(src.type, sa[b].u - sa[a].u, sa[b].v - sa[a].v, src.s0, src.s1, src.s2, kg, ks, d);
+      acc = jadd(acc, jscale(P, c));
+      if (a < b) {
+        T gc = jdot_re(Ja, P);
+        g0 += gc * d[0]; g1 += gc * d[1]; g2 += gc * d[2];
+      }
+    }
+    sgJ[si * S.nap + a] = acc;
+    atomicAdd(&sacc[si * kNAcc + 7], g0);
+    atomicAdd(&sacc[si * kNAcc + 8], g1);
+    atomicAdd(&sacc[si * kNAcc + 9], g2);
+  }
+}
+
+// Chain d chi^2 / dJ through E, K and sqrt(B) to the source parameters.
+template <typename T>
+__device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int ch, int s0, int ns,
+                          const SrcInfo<T>* ss, const AntInfo<T>* sa, const double* sad, const Jones<T>* sgJ,
+                          T* sacc, const ChanPos<T>& cp) {
+  const T f = A.freq[ch];
+  const double nu_over_c = double(f) / kLightSpeed;
+  const double dphase = 2.0 * kPi * nu_over_c;  // |dK/dphi|
+  const T half_log_ratio = T(0.5) * mb_log(f / A.ref_freq[ch]);
+  const BeamGeom G{A.lw, A.mh, A.nud};
+  for (int i = threadIdx.x; i < ns * A.na; i += blockDim.x) {
+    const int si = i / A.na, a = i - si * A.na;
+    const SrcInfo<T>& src = ss[si];
+    const AntInfo<T>& ai = sa[a];
+    const Jones<T> gJ = sgJ[si * S.nap + a];
+    Cx<T> K = phase_term(A, t, s0 + si, a, f, nu_over_c);
+    T l, m;
+    beam_lm<T>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
+    GridPos<T> gl = grid_pos<T>(l, A.ll, A.ul, A.lscale, A.lw);
+    GridPos<T> gm = grid_pos<T>(m, A.lmm, A.um, A.mscale, A.mh);
+    Jones<T> E, dEl, dEm;
+    beam_interp_d<T>(A.E_beam, G, gl, gm, cp, E, dEl, dEm);
+    const Jones<T>& B = src.B;
+    Jones<T> KB = {cmul(K, B.a), cmul(K, B.b), cmul(K, B.c), cmul(K, B.d)};
+    // E
+    Jones<T> gE = jmulh(gJ, KB);
+    T g_ld = gl.inside ? jdot_re(gE, dEl) * A.lscale : T(0);
+    T g_md = gm.inside ? jdot_re(gE, dEm) * A.mscale : T(0);
+    T gl0 = g_ld * ai.sc_l * ai.cos_pa + g_md * ai.sc_m * ai.sin_pa;
+    T gm0 = -g_ld * ai.sc_l * ai.sin_pa + g_md * ai.sc_m * ai.cos_pa;
+    // K and sqrt(B)
+    Jones<T> gKB = jhmul(E, gJ);
+    Cx<T> gK = cmulc(gKB.a, B.a) + cmulc(gKB.b, B.b) + cmulc(gKB.c, B.c) + cmulc(gKB.d, B.d);
+    T gphi = T(dphase) * (gK.r * K.i - gK.i * K.r);
+    double lD = double(src.l), mD = double(src.m);
+    double nfull = sqrt(1.0 - lD * lD - mD * mD);
+    double u = sad[3 * a], v = sad[3 * a + 1], w = sad[3 * a + 2];
+    gl0 += T(double(gphi) * (u - w * lD / nfull));
+    gm0 += T(double(gphi) * (v - w * mD / nfull));
+    Cx<T> Kc = conj(K);
+    Jones<T> gB = {cmul(Kc, gKB.a), cmul(Kc, gKB.b), cmul(Kc, gKB.c), cmul(Kc, gKB.d)};
+    T GB = jdot_re(gB, B);
+    const T det0 = src.I * src.I - src.Q * src.Q - src.U * src.U - src.V * src.V;
+    const T s0v = mb_sqrt(det0 > T(0) ? det0 : T(0));
+    T gI = 0, gQ = 0, gU = 0, gVv = 0;
+    if (s0v > T(0)) {
+      T tt = mb_sqrt(T(2) * src.power * (src.I + s0v));
+      T pt = src.power / tt;
+      T tr1 = gB.a.r + gB.d.r;
+      T q2 = GB / (T(2) * s0v * (src.I + s0v));
+      gI = pt * (T(1) + src.I / s0v) * tr1 - GB / (T(2) * s0v);
+      gQ = pt * ((gB.a.r - gB.d.r) - (src.Q / s0v) * tr1) + q2 * src.Q;
+      gU = pt * ((gB.b.r + gB.c.r) - (src.U / s0v) * tr1) + q2 * src.U;
+      gVv = pt * ((gB.b.i - gB.c.i) - (src.V / s0v) * tr1) + q2 * src.V;
+    }
+    T galpha = GB * half_log_ratio;
+    T* acc = sacc + si * kNAcc;
+    atomicAdd(acc + 0, gl0); atomicAdd(acc + 1, gm0);
+    atomicAdd(acc + 2, gI); atomicAdd(acc + 3, gQ); atomicAdd(acc + 4, gU); atomicAdd(acc + 5, gVv);
+    atomicAdd(acc + 6, galpha);
+  }
+}
+
+template <typename T>
+__device__ void adj_flush(const FusedArgs<T>& A, int t, int s0, int ns, T* sacc) {
+  for (int i = threadIdx.x; i < ns * kNAcc; i += blockDim.x) {
+    const int si = i / kNAcc, k = i - si * kNAcc, s = s0 + si;
+    const double val = double(sacc[i]);
+    sacc[i] = T(0);
+    if (val == 0.0) continue;
+    if (k < 2) atomicAdd(&A.acc_lm[2 * s + k], val);
+    else if (k < 6) atomicAdd(&A.acc_stokes[(size_t(s) * A.ntime + t) * 4 + (k - 2)], val);
+    else if (k == 6) atomicAdd(&A.acc_alpha[size_t(s) * A.ntime + t], val);
+    else {
+      int st = src_type(A, s);
+      if (st == SRC_GAUSS) atomicAdd(&A.acc_gauss[(k - 7) * A.ngsrc + (s - A.npsrc)], val);
+      else if (st == SRC_SERSIC) atomicAdd(&A.acc_sersic[(k - 7) * A.nssrc + (s - A.npsrc - A.ngsrc)], val);
+    }
+  }
+}
+
+template <typename T, int RA, int RS>
+__global__ void __launch_bounds__(kFusedThreads) coh_adj_kernel(FusedArgs<T> A, SmemPlan S) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  AntInfo<T>* sa = reinterpret_cast<AntInfo<T>*>(smem + S.off_ant);
+  double* sad = reinterpret_cast<double*>(smem + S.off_antd);
+  SrcInfo<T>* ss = reinterpret_cast<SrcInfo<T>*>(smem + S.off_src);
+  Jones<T>* sJ = reinterpret_cast<Jones<T>*>(smem + S.off_J);
+  Jones<T>* sgJ = reinterpret_cast<Jones<T>*>(smem + S.off_gJ);
+  Jones<T>* sX = reinterpret_cast<Jones<T>*>(smem + S.off_V);
+  T* sacc = reinterpret_cast<T*>(smem + S.off_acc);
+
+  const int unit = blockIdx.x;
+  const int t = unit / A.nchan, ch = unit - t * A.nchan;
+  load_antennas(A, t, ch, sa, sad);
+  for (int i = threadIdx.x; i < S.npairs; i += blockDim.x) sX[i] = jzero<T>();
+  for (int i = threadIdx.x; i < S.st * kNAcc; i += blockDim.x) sacc[i] = T(0);
+  __syncthreads();
+  for (int bl = threadIdx.x; bl < A.nbl; bl += blockDim.x) {
+    size_t tbl = size_t(t) * A.lnbl + bl;
+    int p = A.ant1[tbl], q = A.ant2[tbl];
+    Jones<T> g = jload<T>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch));
+    if (p <= q) atomic_add_jones(&sX[pair_index(p, q, A.na)], g);
+    else atomic_add_jones(&sX[pair_index(q, p, A.na)], jherm(g));
+  }
+  __syncthreads();
+
+  const T f = A.freq[ch];
+  const ChanPos<T> cp = chan_pos<T>(f, A.lfreq, A.ufreq, A.nud);
+  const T kg = A.gauss_scale * f, ks = A.two_pi_over_c * f;
+  for (int s0 = 0; s0 < A.nsrc;) {
+    int s1 = s0 < A.npsrc ? min(s0 + S.st, A.npsrc) : min(s0 + S.st, A.nsrc);
+    int ns = s1 - s0;
+    load_sources(A, t, ch, s0, ns, ss);
+    __syncthreads();
+    produce_jones(A, S, t, ch, s0, ns, ss, sa, sJ, cp);
+    __syncthreads();
+    if (s0 < A.npsrc) adj_consume_point<T, RA, RS>(A, S, ns, sJ, sX, sgJ);
+    else adj_consume_ext<T>(A, S, ns, ss, sa, sJ, sX, sgJ, sacc, kg, ks);
+    __syncthreads();
+    adj_chain<T>(A, S, t, ch, s0, ns, ss, sa, sad, sgJ, sacc, cp);
+    __syncthreads();
+    adj_flush<T>(A, t, s0, ns, sacc);
+    __syncthreads();
+    s0 = s1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Small kernels: FP64 phase path lengths, gradient finalisation
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void phi_kernel(FusedArgs<T> A, double* __restrict__ phi) {
+  size_t total = size_t(A.ntime) * A.nsrc * A.na;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+    int a = int(i % A.na);
+    int s = int((i / A.na) % A.nsrc);
+    int t = int(i / (size_t(A.na) * A.nsrc));
+    double l = A.lm[2 * s], m = A.lm[2 * s + 1];
+    double n = sqrt(1.0 - l * l - m * m) - 1.0;
+    const T* p = A.uvw + 3 * (size_t(t) * A.lna + a);
+    phi[i] = l * double(p[0]) + m * double(p[1]) + n * double(p[2]);
+  }
+}
+
+template <typename T>
+__global__ void finalize_grads_kernel(FusedArgs<T> A, double scale, T* __restrict__ g_lm, T* __restrict__ g_stokes,
+                                      T* __restrict__ g_alpha, T* __restrict__ g_gauss, T* __restrict__ g_sersic,
+                                      T* __restrict__ g_G) {
+  const size_t n_lm = size_t(A.nsrc) * 2, n_st = size_t(A.nsrc) * A.ntime;
+  const size_t n_g = size_t(3) * A.ngsrc, n_x = size_t(3) * A.nssrc;
+  const size_t n_G = size_t(A.ntime) * A.na * A.nchan;
+  const size_t total = n_lm + n_st + n_g + n_x + n_G;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+    size_t j = i;
+    if (j < n_lm) { if (g_lm) g_lm[j] = T(A.acc_lm[j] * scale); continue; }
+    j -= n_lm;
+    if (j < n_st) {
+      size_t s = j / A.ntime, t = j % A.ntime;
+      size_t dst = s * A.ltime + t;
+      if (g_stokes)
+        for (int k = 0; k < 4; ++k) g_stokes[4 * dst + k] = T(A.acc_stokes[4 * j + k] * scale);
+      if (g_alpha) g_alpha[dst] = T(A.acc_alpha[j] * scale);
+      continue;
+    }
+    j -= n_st;
+    if (j < n_g) { if (g_gauss) g_gauss[(j / A.ngsrc) * A.lgsrc + j % A.ngsrc] = T(A.acc_gauss[j] * scale); continue; }
+    j -= n_g;
+    if (j < n_x) { if (g_sersic) g_sersic[(j / A.nssrc) * A.lssrc + j % A.nssrc] = T(A.acc_sersic[j] * scale); continue; }
+    j -= n_x;
+    if (g_G) {
+      size_t ch = j % A.nchan, a = (j / A.nchan) % A.na, t = j / (size_t(A.nchan) * A.na);
+      const T* src = A.dG + 8 * j;
+      T* dst = g_G + 8 * ((t * A.lna + a) * A.lchan + ch);
+      for (int k = 0; k < 8; ++k) dst[k] = T(double(src[k]) * scale);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct WsLayout {
+  size_t phi, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, tc, total;
+};
+
+WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_grad) {
+  const size_t es = dtype == MB_FLOAT64 ? 8 : 4;
+  const size_t nt = ext(d->ntime), na = ext(d->na), nbl = ext(d->nbl), nc = ext(d->nchan);
+  const size_t ns = ext(d->nsrc), ng = ext(d->ngsrc), nx = ext(d->nssrc);
+  WsLayout L;
+  size_t o = 0;
+  auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 256); return r; };
+  L.phi = take(nt * ns * na * 8);
+  L.partial = take(nt * nc * 8);
+  L.gV = take(want_grad ? nt * nbl * nc * 8 * es : 0);
+  L.dG = take(want_grad ? nt * na * nc * 8 * es : 0);
+  L.acc_lm = take(want_grad ? ns * 2 * 8 : 0);
+  L.acc_stokes = take(want_grad ? ns * nt * 4 * 8 : 0);
+  L.acc_alpha = take(want_grad ? ns * nt * 8 : 0);
+  L.acc_gauss = take(want_grad ? 3 * ng * 8 : 0);
+  L.acc_sersic = take(want_grad ? 3 * nx * 8 : 0);
+  L.acc_end = o;
+  L.tc = take(mode != MB_MODE_NATIVE ? tc_scratch_bytes(d) : 0);
+  L.total = o;
+  return L;
+}
+
+template <typename T>
+mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32_t options,
+                    const mb_rime_inputs* in, void* model_vis, void* chi2, bool want_grad, void* ws,
+                    const WsLayout& L) {
+  A.ntime = ext(d->ntime); A.na = ext(d->na); A.nbl = ext(d->nbl); A.nchan = ext(d->nchan);
+  A.nsrc = ext(d->nsrc); A.npsrc = ext(d->npsrc); A.ngsrc = ext(d->ngsrc); A.nssrc = ext(d->nssrc);
+  A.ltime = d->ntime.local_size; A.lna = d->na.local_size; A.lnbl = d->nbl.local_size;
+  A.lchan = d->nchan.local_size; A.lgsrc = d->ngsrc.local_size; A.lssrc = d->nssrc.local_size;
+  A.lw = d->beam_lw.local_size; A.mh = d->beam_mh.local_size; A.nud = d->beam_nud.local_size;
+  A.t0 = 0; A.ch0 = 0;
+  A.accumulate_in = d->nsrc.lower_extent > 0;
+  A.partial_out = d->nsrc.upper_extent < d->nsrc.global_size;
+  A.weights = options & MB_APPLY_WEIGHTS;
+  A.residuals = options & MB_RESIDUALS;
+  A.want_grad = want_grad;
+  A.ll = T(P->beam_ll); A.lmm = T(P->beam_lm); A.ul = T(P->beam_ul); A.um = T(P->beam_um);
+  A.lfreq = T(P->beam_lfreq); A.ufreq = T(P->beam_ufreq);
+  A.lscale = T(A.lw - 1) / (A.ul - A.ll);
+  A.mscale = T(A.mh - 1) / (A.um - A.lmm);
+  A.gauss_scale = T(P->gauss_scale); A.two_pi_over_c = T(P->two_pi_over_c);
+  A.inv_sigma2 = 1.0 / P->sigma_sqrd;
+  A.uvw = (const T*)in->uvw; A.freq = (const T*)in->frequency; A.ref_freq = (const T*)in->ref_frequency;
+  A.pa = (const T*)in->parallactic_angles; A.pe = (const T*)in->point_errors; A.sc = (const T*)in->antenna_scaling;
+  A.E_beam = (const T*)in->E_beam; A.G = (const T*)in->G_term; A.lm = (const T*)in->lm;
+  A.stokes = (const T*)in->stokes; A.alpha = (const T*)in->alpha; A.gauss = (const T*)in->gauss_shape;
+  A.sersic = (const T*)in->sersic_shape; A.weight = (const T*)in->weight_vector; A.obs = (const T*)in->observed_vis;
+  A.ant1 = in->antenna1; A.ant2 = in->antenna2; A.flag = in->flag;
+  A.model_vis = (T*)model_vis; A.chi2 = (T*)chi2;
+  char* w = static_cast<char*>(ws);
+  A.phi = reinterpret_cast<const double*>(w + L.phi);
+  A.partial = reinterpret_cast<double*>(w + L.partial);
+  A.gV = want_grad ? reinterpret_cast<T*>(w + L.gV) : nullptr;
+  A.dG = want_grad ? reinterpret_cast<T*>(w + L.dG) : nullptr;
+  A.acc_lm = reinterpret_cast<double*>(w + L.acc_lm);
+  A.acc_stokes = reinterpret_cast<double*>(w + L.acc_stokes);
+  A.acc_alpha = reinterpret_cast<double*>(w + L.acc_alpha);
+  A.acc_gauss = reinterpret_cast<double*>(w + L.acc_gauss);
+  A.acc_sersic = reinterpret_cast<double*>(w + L.acc_sersic);
+  A.Vpoint = nullptr;
+  return MB_OK;
+}
+
+mb_status check_inputs(const mb_dims* d, const mb_props* P, uint32_t options, const mb_rime_inputs* in,
+                       const void* model_vis) {
+  MB_CHECK(check_dims(d, true));
+  MB_REQUIRE(P, "props"); MB_REQUIRE(in, "inputs");
+  MB_REQUIRE(in->uvw, "uvw"); MB_REQUIRE(in->antenna1, "antenna1"); MB_REQUIRE(in->antenna2, "antenna2");
+  MB_REQUIRE(in->frequency, "frequency"); MB_REQUIRE(in->ref_frequency, "ref_frequency");
+  MB_REQUIRE(in->parallactic_angles, "parallactic_angles"); MB_REQUIRE(in->point_errors, "point_errors");
+  MB_REQUIRE(in->antenna_scaling, "antenna_scaling"); MB_REQUIRE(in->E_beam, "E_beam");
+  MB_REQUIRE(in->lm, "lm"); MB_REQUIRE(in->stokes, "stokes"); MB_REQUIRE(in->alpha, "alpha");
+  if (ext(d->ngsrc) > 0) MB_REQUIRE(in->gauss_shape, "gauss_shape");
+  if (ext(d->nssrc) > 0) MB_REQUIRE(in->sersic_shape, "sersic_shape");
+  const bool partial_out = d->nsrc.upper_extent < d->nsrc.global_size;
+  if (partial_out || d->nsrc.lower_extent > 0) MB_REQUIRE(model_vis, "model_vis (source batches accumulate in it)");
+  if (!partial_out) {
+    MB_REQUIRE(in->G_term, "G_term"); MB_REQUIRE(in->flag, "flag"); MB_REQUIRE(in->observed_vis, "observed_vis");
+    if (options & MB_APPLY_WEIGHTS) MB_REQUIRE(in->weight_vector, "weight_vector");
+  }
+  if (options & ~(MB_APPLY_WEIGHTS | MB_RESIDUALS)) return fail(MB_ERR_INVALID_ARG, "unknown option bits 0x%x", options);
+  if (!(P->sigma_sqrd > 0.0) && !(options & MB_APPLY_WEIGHTS))
+    return fail(MB_ERR_INVALID_ARG, "sigma_sqrd must be > 0 (got %g)", P->sigma_sqrd);
+  if (ext(d->na) > 0xffff) return fail(MB_ERR_UNSUPPORTED, "na > 65535");
+  return MB_OK;
+}
+
+template <typename T>
+mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* ws, const WsLayout& L,
+                         cudaStream_t stream) {
+  const int units = A.ntime * A.nchan;
+  if (units == 0) {
+    MB_CUDA(cudaMemsetAsync(X2, 0, sizeof(double), stream));
+    return MB_OK;
+  }
+  {
+    size_t n = size_t(A.ntime) * A.nsrc * A.na;
+    if (n > 0) {
+      int blocks = int(std::min<size_t>((n + 255) / 256, 1u << 20));
+      phi_kernel<T><<<blocks, 256, 0, stream>>>(A, reinterpret_cast<double*>(static_cast<char*>(ws) + L.phi));
+      MB_CHECK(check_launch("phi_kernel"));
+    }
+  }
+  FusedArgs<T> B = A;
+  if constexpr (sizeof(T) == 4) {
+    if (mode != MB_MODE_NATIVE && A.npsrc > 0) {
+      float* Vp = reinterpret_cast<float*>(static_cast<char*>(ws) + L.tc);
+      MB_CHECK(tc_point_coherencies(A, mode, Vp, stream));
+      B.Vpoint = Vp;
+    }
+  }
+  constexpr int RP = FwdTile<T>::RP, RQ = FwdTile<T>::RQ;
+  SmemPlan S = make_plan<T>(A.na, false);
+  if (S.total > 227 * 1024)
+    return fail(MB_ERR_UNSUPPORTED, "fused forward needs %zu bytes of shared memory for na=%d (max 232448)",
+                S.total, A.na);
+  auto kern = coh_fwd_kernel<T, RP, RQ>;
+  MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
+  kern<<<units, kFusedThreads, S.total, stream>>>(B, S);
+  MB_CHECK(check_launch("coh_fwd_kernel"));
+  const double scale = A.weights ? 1.0 : A.inv_sigma2;
+  sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, scale, X2);
+  return check_launch("sum_partials_kernel");
+}
+
+template <typename T>
+mb_status launch_adjoint(const FusedArgs<T>& A, double grad_scale, const mb_rime_grads* g, void* ws,
+                         const WsLayout& L, cudaStream_t stream) {
+  char* w = static_cast<char*>(ws);
+  MB_CUDA(cudaMemsetAsync(w + L.acc_lm, 0, L.acc_end - L.acc_lm, stream));
+  const int units = A.ntime * A.nchan;
+  if (units > 0 && A.nsrc > 0) {
+    constexpr int RA = AdjTile<T>::RA, RS = AdjTile<T>::RS;
+    SmemPlan S = make_plan<T>(A.na, true);
+    if (S.total > 227 * 1024)
+      return fail(MB_ERR_UNSUPPORTED, "fused adjoint needs %zu bytes of shared memory for na=%d", S.total, A.na);
+    auto kern = coh_adj_kernel<T, RA, RS>;
+    MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
+    kern<<<units, kFusedThreads, S.total, stream>>>(A, S);
+    MB_CHECK(check_launch("coh_adj_kernel"));
+  }
+  size_t total = size_t(A.nsrc) * 2 + size_t(A.nsrc) * A.ntime + 3 * size_t(A.ngsrc) + 3 * size_t(A.nssrc) +
+                 size_t(A.ntime) * A.na * A.nchan;
+  if (total > 0) {
+    int blocks = int(std::min<size_t>((total + 255) / 256, 1u << 16));
+    finalize_grads_kernel<T><<<blocks, 256, 0, stream>>>(A, grad_scale, (T*)g->lm, (T*)g->stokes, (T*)g->alpha,
+                                                         (T*)g->gauss_shape, (T*)g->sersic_shape, (T*)g->G_term);
+    MB_CHECK(check_launch("finalize_grads_kernel"));
+  }
+  return MB_OK;
+}
+
+}  // namespace
+
+size_t fused_workspace_size(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_grad) {
+  return ws_layout(dtype, mode, d, want_grad).total;
+}
+
+}  // namespace mb
+
+using namespace mb;
+
+extern "C" {
+
+size_t mb_rime_workspace_size(mb_dtype dtype, mb_mode mode, const mb_dims* dims, int want_grad) {
+  if (check_dims(dims, true) != MB_OK) return 0;
+  return fused_workspace_size(dtype, mode, dims, want_grad != 0);
+}
+
+mb_status mb_rime_forward(mb_dtype dtype, mb_mode mode, const mb_dims* dims, const mb_props* props,
+                          uint32_t options, const mb_rime_inputs* in, void* model_vis, void* chi_sqrd_result,
+                          double* X2, int want_grad, void* workspace, size_t workspace_bytes, void* stream) {
+  MB_CHECK(check_inputs(dims, props, options, in, model_vis));
+  MB_REQUIRE(X2, "X2");
+  if (dtype != MB_FLOAT32 && dtype != MB_FLOAT64) return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
+  if (mode != MB_MODE_NATIVE && mode != MB_MODE_SPLIT_TF32 && mode != MB_MODE_SPLIT_BF16)
+    return fail(MB_ERR_INVALID_ARG, "mode %d", int(mode));
+  if (mode != MB_MODE_NATIVE && dtype != MB_FLOAT32)
+    return fail(MB_ERR_UNSUPPORTED, "split-precision modes take FLOAT32 data");
+  const bool grad = want_grad != 0;
+  if (grad && dims->nsrc.upper_extent < dims->nsrc.global_size)
+    return fail(MB_ERR_INVALID_ARG, "gradients need the last source batch (upper_extent == global_size)");
+  WsLayout L = ws_layout(dtype, mode, dims, grad);
+  if (workspace == nullptr || workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return fail(MB_ERR_WORKSPACE, "workspace must be >= %zu bytes and 256-byte aligned (got %zu)", L.total,
+                workspace_bytes);
+  cudaStream_t s = as_stream(stream);
+  if (dtype == MB_FLOAT32) {
+    FusedArgs<float> A;
+    fill_args(A, dims, props, options, in, model_vis, chi_sqrd_result, grad, workspace, L);
+    return launch_forward(A, mode, X2, workspace, L, s);
+  }
+  FusedArgs<double> A;
+  fill_args(A, dims, props, options, in, model_vis, chi_sqrd_result, grad, workspace, L);
+  return launch_forward(A, mode, X2, workspace, L, s);
+}
+
+mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims, const mb_props* props,
+                          uint32_t options, const mb_rime_inputs* in, double grad_scale, const mb_rime_grads* grads,
+                          void* workspace, size_t workspace_bytes, void* stream) {
+  MB_CHECK(check_inputs(dims, props, options, in, nullptr));
+  MB_REQUIRE(grads, "grads");
+  if (dtype != MB_FLOAT32 && dtype != MB_FLOAT64) return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
+  if (dims->nsrc.lower_extent > 0 || dims->nsrc.upper_extent < dims->nsrc.global_size)
+    return fail(MB_ERR_INVALID_ARG, "the adjoint takes the whole source set in one call");
+  WsLayout L = ws_layout(dtype, mode, dims, true);
+  if (workspace == nullptr || workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return fail(MB_ERR_WORKSPACE, "workspace must be >= %zu bytes and 256-byte aligned (got %zu)", L.total,
+                workspace_bytes);
+  cudaStream_t s = as_stream(stream);
+  if (dtype == MB_FLOAT32) {
+    FusedArgs<float> A;
+    fill_args(A, dims, props, options, in, nullptr, nullptr, true, workspace, L);
+    return launch_adjoint(A, grad_scale, grads, workspace, L, s);
+  }
+  FusedArgs<double> A;
+  fill_args(A, dims, props, options, in, nullptr, nullptr, true, workspace, L);
+  return launch_adjoint(A, grad_scale, grads, workspace, L, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,70 @@
+// Parameters and shared-memory plan of the fused per-(time, channel)
+// kernels.  Shared between the CUDA-core kernels (mb_fused.cu) and the
+// tensor-core point-source kernels (mb_tc.cu).
+#pragma once
+
+#include "mb_common.cuh"
+#include "mb_internal.h"
+
+namespace mb {
+
+template <typename T>
+struct FusedArgs {
+  // active extents and local strides
+  int ntime, na, nbl, nchan, nsrc, npsrc, ngsrc, nssrc;
+  int ltime, lna, lnbl, lchan, lgsrc, lssrc;
+  int lw, mh, nud;
+  int t0, ch0;  // first (time, channel) unit handled by this launch
+  bool accumulate_in, partial_out, weights, residuals, want_grad;
+  T ll, lmm, ul, um, lfreq, ufreq, lscale, mscale, gauss_scale, two_pi_over_c;
+  double inv_sigma2;
+  // inputs
+  const T *uvw, *freq, *ref_freq, *pa, *pe, *sc, *E_beam, *G, *lm, *stokes, *alpha, *gauss, *sersic,
+      *weight, *obs;
+  const int32_t *ant1, *ant2;
+  const uint8_t* flag;
+  // outputs
+  T* model_vis;
+  T* chi2;
+  // workspace
+  const double* phi;  // (ntime, nsrc, na) FP64 phase path lengths
+  double* partial;    // (ntime * nchan) chi^2 partial sums
+  T* gV;              // (ntime, nbl, nchan, 4) complex d chi^2 / d V
+  T* dG;              // (ntime, na, nchan, 4) complex d chi^2 / d G
+  // adjoint accumulators (FP64)
+  double *acc_lm, *acc_stokes, *acc_alpha, *acc_gauss, *acc_sersic;
+  // the point-source coherencies come from the tensor-core kernel
+  const float* Vpoint;  // (ntime*nchan, na*na) packed by mb_tc.cu, or NULL
+};
+
+// Per-antenna data for one (time, channel) unit.
+template <typename T>
+struct AntInfo {
+  T sin_pa, cos_pa, pe_l, pe_m, sc_l, sc_m, u, v;
+};
+
+// Per-source data for one (time, channel) unit.
+template <typename T>
+struct SrcInfo {
+  Jones<T> B;        // sqrt of the brightness matrix at this channel
+  T l, m;            // direction cosines
+  T s0, s1, s2;      // shape parameters (gaussian el, em, R / sersic e1, e2, R)
+  T power, I, Q, U, V;
+  int type;
+  int pad;
+};
+
+// Byte offsets of the dynamic shared-memory regions of one CTA.
+struct SmemPlan {
+  int nap;          // antennas padded to the register tile
+  int st;           // sources per tile
+  int npairs;       // na (na + 1) / 2
+  int nitems;       // pair tiles
+  size_t off_ant, off_antd, off_src, off_J, off_gJ, off_V, off_items, off_acc, off_red, total;
+};
+
+constexpr int kFusedThreads = 256;
+
+size_t fused_workspace_size(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_grad);
+
+}  // namespace mb

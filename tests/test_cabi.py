@@ -1,0 +1,88 @@
+"""The C ABI library: builds, loads and exports every declared symbol;
+argument validation fails cleanly without touching the GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, 'include', 'montblanc_gb300.h')
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r'^\s*(?:const char\*|mb_status|size_t)\s+(mb_\w+)\s*\(', text, re.M)))
+
+
+def test_header_declares_entry_points():
+    fns = declared_functions()
+    for f in ('mb_bsqrt', 'mb_ebeam', 'mb_ekb_sqrt', 'mb_sum_coherencies', 'mb_reduce_chi2',
+              'mb_rime_forward', 'mb_rime_adjoint', 'mb_rime_workspace_size', 'mb_last_error_string'):
+        assert f in fns
+
+
+def test_library_exports_every_declared_symbol():
+    from montblanc_gb300 import _cabi
+    lib = ctypes.CDLL(_cabi.lib_path())
+    for f in declared_functions():
+        assert hasattr(lib, f), f
+    assert set(declared_functions()) == set(_cabi.exported_symbols())
+    assert 'sm_103a' in _cabi.version()
+
+
+def test_null_pointer_is_rejected():
+    from montblanc_gb300 import _cabi
+    d = _cabi.make_dims(2, 3, 3, 4, 2)
+    st = _cabi.lib.mb_bsqrt(_cabi.MB_FLOAT64, ctypes.byref(d), None, None, None, None, None, None)
+    assert _cabi.STATUS_NAMES[st] == 'MB_ERR_NULL_PTR'
+    assert b'stokes' in _cabi.lib.mb_last_error_string()
+
+
+def test_bad_extent_is_rejected():
+    from montblanc_gb300 import _cabi
+    d = _cabi.make_dims(2, 3, 3, 4, 2, extents={'ntime': (1, 5)})
+    fake = ctypes.c_void_p(16)
+    st = _cabi.lib.mb_bsqrt(_cabi.MB_FLOAT64, ctypes.byref(d), fake, fake, fake, fake, fake, None)
+    assert _cabi.STATUS_NAMES[st] == 'MB_ERR_BAD_EXTENT'
+
+
+def test_bad_shape_and_dtype_are_rejected():
+    from montblanc_gb300 import _cabi
+    d = _cabi.make_dims(2, 3, 3, 4, 2)
+    d.npolchan.local_size = d.npolchan.global_size = 7
+    d.npolchan.upper_extent = 7
+    fake = ctypes.c_void_p(16)
+    st = _cabi.lib.mb_bsqrt(_cabi.MB_FLOAT64, ctypes.byref(d), fake, fake, fake, fake, fake, None)
+    assert _cabi.STATUS_NAMES[st] == 'MB_ERR_BAD_SHAPE'
+    d = _cabi.make_dims(2, 3, 3, 4, 2)
+    st = _cabi.lib.mb_bsqrt(7, ctypes.byref(d), fake, fake, fake, fake, fake, None)
+    assert _cabi.STATUS_NAMES[st] == 'MB_ERR_UNSUPPORTED_DTYPE'
+
+
+def test_workspace_is_checked():
+    from montblanc_gb300 import _cabi
+    d = _cabi.make_dims(2, 3, 3, 4, 2, beam=(2, 2, 2))
+    n = _cabi.lib.mb_rime_workspace_size(_cabi.MB_FLOAT32, 0, ctypes.byref(d), 1)
+    assert n > 0
+    assert _cabi.lib.mb_rime_workspace_size(_cabi.MB_FLOAT32, 0, ctypes.byref(d), 0) < n
+    fake = ctypes.c_void_p(256)
+    inp = _cabi.MbRimeInputs()
+    for name in _cabi.INPUT_NAMES:
+        setattr(inp, name, 256)
+    p = _cabi.make_props(gauss_scale=1, two_pi_over_c=1, sigma_sqrd=1, beam_ll=-1, beam_lm=-1,
+                         beam_lfreq=1, beam_ul=1, beam_um=1, beam_ufreq=2)
+    x2 = ctypes.c_void_p(256)
+    st = _cabi.lib.mb_rime_forward(_cabi.MB_FLOAT32, 0, ctypes.byref(d), ctypes.byref(p), 0, ctypes.byref(inp),
+                                   None, None, x2, 1, fake, n - 1, None)
+    assert _cabi.STATUS_NAMES[st] == 'MB_ERR_WORKSPACE'
+    st = _cabi.lib.mb_rime_forward(_cabi.MB_FLOAT64, 1, ctypes.byref(d), ctypes.byref(p), 0, ctypes.byref(inp),
+                                   None, None, x2, 0, fake, 1 << 30, None)
+    assert _cabi.STATUS_NAMES[st] == 'MB_ERR_UNSUPPORTED'
+
+
+def test_python_error_mapping():
+    from montblanc_gb300 import _cabi
+    d = _cabi.make_dims(2, 3, 3, 4, 2)
+    with pytest.raises(_cabi.MontblancError, match='MB_ERR_NULL_PTR'):
+        _cabi.call('mb_bsqrt', _cabi.MB_FLOAT64, ctypes.byref(d), None, None, None, None, None, None)

@@ -1,0 +1,94 @@
+"""Fused forward (mb_rime_forward) against the reference's outputs."""
+import numpy as np
+import pytest
+
+import golden_io
+from gpu_helpers import TOL, solver_for
+from oracle import rime_v4 as O
+
+pytestmark = pytest.mark.gpu
+DTYPES = ('double', 'float')
+CASES = [n for n in golden_io.names() if n != 'given_jones']
+
+
+@pytest.mark.parametrize('dtype', DTYPES)
+@pytest.mark.parametrize('name', CASES)
+def test_fused_solver_matches_reference(name, dtype):
+    import montblanc_gb300 as mb
+    P, ref = golden_io.load(name)
+    with solver_for(P, dtype, mb.Pipeline([mb.RimeV4Fused()])) as s:
+        s.solve()
+        assert golden_io.rel_err(s.retrieve_model_vis(), ref['vis_out']) < TOL[dtype]['vis']
+        assert golden_io.rel_err(s.retrieve_chi_sqrd_result(), ref['chi_sqrd_terms']) < TOL[dtype]['terms']
+        assert abs(s.X2 - ref['X2']) <= TOL[dtype]['X2'] * abs(ref['X2'])
+
+
+@pytest.mark.parametrize('dtype', DTYPES)
+def test_fused_chi2_only(dtype):
+    """model_vis and chi_sqrd_result may be omitted (NULL)."""
+    from montblanc_gb300.rime import RimeProblem
+    P, ref = golden_io.load('small_fp64')
+    prob = RimeProblem.from_numpy(P, dtype=dtype)
+    x2 = prob.forward().item()
+    assert abs(x2 - ref['X2']) <= TOL[dtype]['X2'] * abs(ref['X2'])
+
+
+@pytest.mark.parametrize('dtype', DTYPES)
+def test_fused_source_batches(dtype):
+    """Fused forward over two source batches accumulating in model_vis."""
+    import montblanc_gb300 as mb
+    from montblanc_gb300.rime import RimeProblem
+    from montblanc_gb300 import _cabi
+    import ctypes
+    import torch
+    P, ref = golden_io.load('perm_p3_g3_s3_w0')
+    prob = RimeProblem.from_numpy(P, dtype=dtype)
+    vis = prob.empty_vis()
+    chi2 = prob.empty_chi2()
+    x2 = torch.zeros(1, dtype=torch.float64, device='cuda')
+    ws = prob.workspace('native', False)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for lo, hi, ext in ((0, 4, {'npsrc': (0, 3), 'ngsrc': (0, 1), 'nssrc': (0, 0)}),
+                        (4, 9, {'npsrc': (0, 0), 'ngsrc': (0, 2), 'nssrc': (0, 3)})):
+        # present the batch's sources at the front of each parameter array
+        sl = slice(lo, hi)
+        ov = {'lm': prob.arrays['lm'][sl].contiguous(), 'stokes': prob.arrays['stokes'][sl].contiguous(),
+              'alpha': prob.arrays['alpha'][sl].contiguous()}
+        gl = max(lo, 3) - 3
+        gs = torch.zeros_like(prob.arrays['gauss_shape'])  # keeps the local row stride of 3
+        gs[:, :3 - gl] = prob.arrays['gauss_shape'][:, gl:]
+        ov['gauss_shape'] = gs
+        e = dict(ext)
+        e['nsrc'] = (lo, hi)
+        d = _cabi.make_dims(prob.ntime, prob.na, prob.nbl, prob.nchan, 3, 3, 3, beam=prob.beam,
+                            extents=e, globals_={'nsrc': 9})
+        d.nsrc.local_size = 9
+        inp = prob.inputs(**ov)
+        _cabi.call('mb_rime_forward', prob.mb_dtype, 0, ctypes.byref(d), ctypes.byref(prob.mb_props()),
+                   prob.options(), ctypes.byref(inp), vis.data_ptr(), chi2.data_ptr(), x2.data_ptr(), 0,
+                   ws.data_ptr(), ws.numel(), stream)
+    assert golden_io.rel_err(vis.cpu().numpy(), ref['vis_out']) < TOL[dtype]['vis']
+    assert abs(x2.item() - ref['X2']) <= TOL[dtype]['X2'] * abs(ref['X2'])
+
+
+def test_fused_non_default_antenna_pairs():
+    """Baselines in arbitrary order, including swapped (q, p) pairs and an
+    autocorrelation, against the oracle (which follows antenna1/antenna2)."""
+    from montblanc_gb300.rime import RimeProblem
+    P, _ = golden_io.load('perm_p3_g3_s3_w1')
+    rng = np.random.default_rng(11)
+    a1, a2 = P['antenna1'].copy(), P['antenna2'].copy()
+    for t in range(a1.shape[0]):
+        perm = rng.permutation(a1.shape[1])
+        a1[t], a2[t] = a1[t][perm], a2[t][perm]
+        swap = rng.random(a1.shape[1]) < 0.5
+        a1[t][swap], a2[t][swap] = a2[t][swap].copy(), a1[t][swap].copy()
+        a2[t][0] = a1[t][0]  # one autocorrelation per time step
+    P['antenna1'], P['antenna2'] = a1, a2
+    out, terms, X2 = O.forward(P, src_chunk=9)
+    prob = RimeProblem.from_numpy(P, dtype='double')
+    vis, chi2 = prob.empty_vis(), prob.empty_chi2()
+    x2 = prob.forward(model_vis=vis, chi_sqrd_result=chi2).item()
+    assert golden_io.rel_err(vis.cpu().numpy(), out) < 1e-10
+    assert golden_io.rel_err(chi2.cpu().numpy(), terms) < 1e-10
+    assert abs(x2 - X2) <= 1e-10 * abs(X2)
