@@ -258,7 +258,8 @@ __device__ __forceinline__ GridPos<T> grid_pos(T x, T lower, T upper, T scale, i
   g.inside = (v > T(0)) && (v < T(n - 1));
   v = mb_clamp(v, T(0), T(n - 1));
   T f0 = mb_floor(v);
-  g.i0 = static_cast<int>(f0);
+  // The integer clamp keeps a NaN coordinate (invalid input) inside the cube.
+  g.i0 = min(max(static_cast<int>(f0), 0), n - 1);
   g.i1 = min(g.i0 + 1, n - 1);
   g.d = v - f0;
   return g;
@@ -277,7 +278,7 @@ __device__ __forceinline__ ChanPos<T> chan_pos(T freq, T lfreq, T ufreq, int nud
   v = mb_clamp(v, T(0), T(nud - 1));
   T f0 = mb_floor(v);
   ChanPos<T> c;
-  c.c0 = static_cast<int>(f0);
+  c.c0 = min(max(static_cast<int>(f0), 0), nud - 1);
   c.c1 = min(c.c0 + 1, nud - 1);
   c.d = v - f0;
   return c;

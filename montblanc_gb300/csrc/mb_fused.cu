@@ -199,8 +199,16 @@ __device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const J
   for (int bl = threadIdx.x; bl < A.nbl; bl += blockDim.x) {
     size_t tbl = size_t(t) * A.lnbl + bl;
     int p = A.ant1[tbl], q = A.ant2[tbl];
-    Jones<T> V = p <= q ? sV[pair_index(p, q, A.na)] : jherm(sV[pair_index(q, p, A.na)]);
     size_t vidx = tbl * A.lchan + ch;
+    if (p < 0 || p >= A.na || q < 0 || q >= A.na) {  // invalid antenna index: NaN output
+      const T nan = T(NAN);
+      if (A.model_vis) jstore(A.model_vis + 8 * vidx, Jones<T>{{nan, nan}, {nan, nan}, {nan, nan}, {nan, nan}});
+      if (A.chi2 && !A.partial_out) A.chi2[vidx] = nan;
+      part += double(nan);
+      if (A.want_grad) jstore(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch), jzero<T>());
+      continue;
+    }
+    Jones<T> V = p <= q ? sV[pair_index(p, q, A.na)] : jherm(sV[pair_index(q, p, A.na)]);
     if (A.accumulate_in) V = jadd(V, jload<T>(A.model_vis + 8 * vidx));
     if (A.partial_out) {
       jstore(A.model_vis + 8 * vidx, V);
@@ -611,6 +619,7 @@ __global__ void __launch_bounds__(kFusedThreads) coh_adj_kernel(FusedArgs<T> A, 
   for (int bl = threadIdx.x; bl < A.nbl; bl += blockDim.x) {
     size_t tbl = size_t(t) * A.lnbl + bl;
     int p = A.ant1[tbl], q = A.ant2[tbl];
+    if (p < 0 || p >= A.na || q < 0 || q >= A.na) continue;
     Jones<T> g = jload<T>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch));
     if (p <= q) atomic_add_jones(&sX[pair_index(p, q, A.na)], g);
     else atomic_add_jones(&sX[pair_index(q, p, A.na)], jherm(g));
@@ -781,6 +790,9 @@ mb_status check_inputs(const mb_dims* d, const mb_props* P, uint32_t options, co
   if (!(P->sigma_sqrd > 0.0) && !(options & MB_APPLY_WEIGHTS))
     return fail(MB_ERR_INVALID_ARG, "sigma_sqrd must be > 0 (got %g)", P->sigma_sqrd);
   if (ext(d->na) > 0xffff) return fail(MB_ERR_UNSUPPORTED, "na > 65535");
+  MB_ALIGNED(in->E_beam, 16, "E_beam"); MB_ALIGNED(in->G_term, 16, "G_term");
+  MB_ALIGNED(in->observed_vis, 16, "observed_vis"); MB_ALIGNED(model_vis, 16, "model_vis");
+  MB_ALIGNED(in->flag, 4, "flag");
   return MB_OK;
 }
 

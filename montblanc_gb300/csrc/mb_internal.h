@@ -53,4 +53,14 @@ inline mb_status check_launch(const char* what) {
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Arrays read with vector loads must be aligned: complex Jones arrays to
+// 16 bytes, flags to 4 bytes.
+inline bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
+
+#define MB_ALIGNED(ptr, a, name)                                                            \
+  do {                                                                                      \
+    if ((ptr) != nullptr && !::mb::aligned((ptr), (a)))                                     \
+      return ::mb::fail(MB_ERR_INVALID_ARG, "%s must be %d-byte aligned", name, int(a));   \
+  } while (0)
+
 }  // namespace mb

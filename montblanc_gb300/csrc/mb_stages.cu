@@ -139,6 +139,12 @@ __global__ void sumcoh_kernel(StageDims D, mb_props P, const T* __restrict__ uvw
   size_t tbl = size_t(t) * D.lnbl + bl;
   int p = ant1[tbl], q = ant2[tbl];
   size_t vidx = tbl * D.lchan + ch;
+  if (p < 0 || p >= D.lna || q < 0 || q >= D.lna) {  // invalid antenna index: NaN output
+    const T nan = T(NAN);
+    jstore(vis + 8 * vidx, Jones<T>{{nan, nan}, {nan, nan}, {nan, nan}, {nan, nan}});
+    if (!D.partial_out) chi2[vidx] = nan;
+    return;
+  }
 
   Jones<T> V = jzero<T>();
   if (D.accumulate_in) V = jload<T>(vis + 8 * vidx);
@@ -257,6 +263,7 @@ mb_status mb_bsqrt(mb_dtype dtype, const mb_dims* dims, const void* stokes, cons
   MB_CHECK(check_dims(dims, false));
   MB_REQUIRE(stokes, "stokes"); MB_REQUIRE(alpha, "alpha"); MB_REQUIRE(frequency, "frequency");
   MB_REQUIRE(ref_frequency, "ref_frequency"); MB_REQUIRE(B_sqrt, "B_sqrt");
+  MB_ALIGNED(B_sqrt, 16, "B_sqrt");
   StageDims D = stage_dims(dims);
   size_t n = size_t(D.nsrc) * D.ntime * D.nchan;
   if (n == 0) return MB_OK;
@@ -278,6 +285,7 @@ mb_status mb_ebeam(mb_dtype dtype, const mb_dims* dims, const mb_props* props, c
   MB_REQUIRE(props, "props"); MB_REQUIRE(lm, "lm"); MB_REQUIRE(parallactic_angles, "parallactic_angles");
   MB_REQUIRE(point_errors, "point_errors"); MB_REQUIRE(antenna_scaling, "antenna_scaling");
   MB_REQUIRE(frequency, "frequency"); MB_REQUIRE(E_beam, "E_beam"); MB_REQUIRE(jones, "jones");
+  MB_ALIGNED(E_beam, 16, "E_beam"); MB_ALIGNED(jones, 16, "jones");
   StageDims D = stage_dims(dims);
   size_t n = size_t(D.ntime) * D.na * D.nchan;
   if (n == 0 || D.nsrc == 0) return MB_OK;
@@ -299,6 +307,7 @@ mb_status mb_ekb_sqrt(mb_dtype dtype, const mb_dims* dims, const mb_props* props
   MB_CHECK(check_dims(dims, false));
   MB_REQUIRE(props, "props"); MB_REQUIRE(uvw, "uvw"); MB_REQUIRE(lm, "lm");
   MB_REQUIRE(frequency, "frequency"); MB_REQUIRE(B_sqrt, "B_sqrt"); MB_REQUIRE(jones, "jones");
+  MB_ALIGNED(B_sqrt, 16, "B_sqrt"); MB_ALIGNED(jones, 16, "jones");
   StageDims D = stage_dims(dims);
   size_t n = size_t(D.ntime) * D.na * D.nchan;
   if (n == 0 || D.nsrc == 0) return MB_OK;
@@ -332,6 +341,8 @@ mb_status mb_sum_coherencies(mb_dtype dtype, const mb_dims* dims, const mb_props
     if (options & MB_APPLY_WEIGHTS) MB_REQUIRE(weight_vector, "weight_vector");
   }
   if (options & ~(MB_APPLY_WEIGHTS | MB_RESIDUALS)) return fail(MB_ERR_INVALID_ARG, "unknown option bits 0x%x", options);
+  MB_ALIGNED(jones, 16, "jones"); MB_ALIGNED(observed_vis, 16, "observed_vis"); MB_ALIGNED(G_term, 16, "G_term");
+  MB_ALIGNED(model_vis, 16, "model_vis"); MB_ALIGNED(flag, 4, "flag");
   size_t n = size_t(D.ntime) * D.nbl * D.nchan;
   if (n == 0) return MB_OK;
   cudaStream_t s = as_stream(stream);
