@@ -155,14 +155,16 @@ def jones_mul(A, B):
     """2x2 product of row-major [00,01,10,11] Jones arrays (CPUSolver.py:518-541)."""
     a = A.reshape(A.shape[:-1] + (2, 2))
     b = B.reshape(B.shape[:-1] + (2, 2))
-    return np.matmul(a, b).reshape(A.shape)
+    r = np.matmul(a, b)
+    return r.reshape(r.shape[:-2] + (4,))
 
 
 def jones_mul_h(A, B):
     """A @ B^H for row-major Jones arrays (CPUSolver.py:529-531)."""
     a = A.reshape(A.shape[:-1] + (2, 2))
     b = B.reshape(B.shape[:-1] + (2, 2))
-    return np.matmul(a, np.conj(np.swapaxes(b, -1, -2))).reshape(A.shape)
+    r = np.matmul(a, np.conj(np.swapaxes(b, -1, -2)))
+    return r.reshape(r.shape[:-2] + (4,))
 
 
 def ekb_sqrt_per_antenna(P, srcs=None, times=None):
