@@ -1,0 +1,447 @@
+#!/usr/bin/env python
+"""Benchmark: source.vis terms/s of the RIME v4 chi^2 + full gradient.
+
+One step = one fused forward chi^2 (mb_rime_forward, want_grad=1) plus the
+adjoint (mb_rime_adjoint) over the whole workload, inputs resident on the
+GPU.  terms/step = nsrc * ntime * nbl * nchan.
+
+Default workload (the largest one of the suite, and the one the
+split-precision target is stated on): 200 time steps, 64 antennas
+(2016 baselines), 256 channels, 20000 point + 500 gaussian sources, FP32
+data, unit weights, no flags; observed = model + N(0, 0.1) complex noise.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--mode MODE]
+                    [--workload NAME] [--impl reference]
+
+With --gpus N > 1 (one process per GPU under torch.distributed.run) every
+rank evaluates its own replica of the workload: the path needs no
+collective, so the job total is N * terms / (max over ranks of the time).
+
+Prints one JSON line (rank 0).
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'source·vis terms/s for χ²+grad, split-prec vs plain FP32, at stated FP64 error'
+UNIT = 'source·vis terms/s'
+
+# Algorithmic work per source.vis term: a 2x2 complex J_p J_q^H product with
+# accumulation (64 flops) forward; the two 2x2 complex products of the
+# adjoint, d/dJ_p += gV J_q and d/dJ_q += gV^H J_p (128 flops).
+FLOPS_FWD = 64
+FLOPS_ADJ = 128
+SM_COUNT = 152
+
+# DRAM traffic per launch of the dominant kernel from ncu captures, keyed by
+# (kernel, workload).  Captures: profiles/*.md (command lines given there).
+NCU_TRAFFIC = {}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=3)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
+    ap.add_argument('--workload', default='large_point')
+    ap.add_argument('--mode', default='native', help="native | split_tf32 | split_bf16")
+    ap.add_argument('--compare-plain', action='store_true', help='also time the plain FP32 form')
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--seed', type=int, default=20261203)
+    return ap.parse_args()
+
+
+def workload_desc(name):
+    from montblanc_gb300 import synth
+    w = synth.WORKLOADS[name]
+    nbl = synth.nr_of_baselines(w['na'])
+    return ('%s: ntime %d, na %d (nbl %d), nchan %d, %d point + %d gaussian + %d sersic sources, FP32 data'
+            % (name, w['ntime'], w['na'], nbl, w['nchan'], w['npsrc'], w['ngsrc'], w['nssrc']))
+
+
+def terms_of(name):
+    from montblanc_gb300 import synth
+    w = synth.WORKLOADS[name]
+    return (w['npsrc'] + w['ngsrc'] + w['nssrc']) * w['ntime'] * synth.nr_of_baselines(w['na']) * w['nchan']
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing
+# ---------------------------------------------------------------------------
+def dist_init(n):
+    import torch
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device='cuda')
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler
+# ---------------------------------------------------------------------------
+class Clocks(object):
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self):
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        idx = os.environ.get('CUDA_VISIBLE_DEVICES', '0').split(',')[0] or '0'
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', idx, '--query-gpu=' + self.FIELDS,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap')
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(',')]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith('active'):
+                    reasons.add(n)
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': smax,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def build_workload(name, seed):
+    import torch
+    from montblanc_gb300 import synth
+    from montblanc_gb300.rime import RimeProblem
+    spec = synth.WORKLOADS[name]
+    P = synth.make_problem(**spec, seed=seed, vis_arrays=False)
+    prob = RimeProblem.from_numpy(P, dtype='float', device='cuda')
+    model = prob.empty_vis()
+    prob.forward(mode='native', model_vis=model)
+    g = torch.Generator(device='cuda')
+    g.manual_seed(seed + 1)
+    noise = torch.randn(model.shape, dtype=torch.complex64, device='cuda', generator=g)
+    model.add_(noise, alpha=0.1 * math.sqrt(2.0))  # N(0, 0.1) on re and im
+    prob.arrays['observed_vis'] = model
+    torch.cuda.synchronize()
+    return P, prob
+
+
+def subset_problem(P, prob, times, chans):
+    """The same sky and antennas on a few (time, channel) units, for the
+    error measurement against the FP64 path."""
+    import numpy as np
+    Q = dict(P)
+    t = np.asarray(times)
+    c = np.asarray(chans)
+    Q['uvw'] = P['uvw'][t]
+    Q['parallactic_angles'] = P['parallactic_angles'][t]
+    Q['antenna1'] = P['antenna1'][t]
+    Q['antenna2'] = P['antenna2'][t]
+    Q['frequency'] = P['frequency'][c]
+    Q['ref_frequency'] = P['ref_frequency'][c]
+    Q['point_errors'] = P['point_errors'][t][:, :, c]
+    Q['antenna_scaling'] = P['antenna_scaling'][:, c]
+    Q['G_term'] = P['G_term'][t][:, :, c]
+    Q['stokes'] = P['stokes'][:, t]
+    Q['alpha'] = P['alpha'][:, t]
+    obs = prob.arrays['observed_vis'][t][:, :, c].cpu().numpy()
+    Q['observed_vis'] = obs
+    Q['flag'] = np.zeros(obs.shape, np.uint8)
+    return Q
+
+
+def errors_vs_fp64(P, prob, mode):
+    """Visibility, chi^2 and gradient errors of ``mode`` against the FP64
+    GPU path (itself within 1e-10 of the reference CPU path) on 2 time steps
+    x 3 channels of the workload with every source and antenna."""
+    import numpy as np
+    import torch
+    from montblanc_gb300.rime import RimeProblem
+    Q = subset_problem(P, prob, [0, prob.ntime - 1], [0, prob.nchan // 2, prob.nchan - 1])
+    p64 = RimeProblem.from_numpy(Q, dtype='double')
+    p32 = RimeProblem.from_numpy(Q, dtype='float')
+    v64, v32 = p64.empty_vis(), p32.empty_vis()
+    x64, g64 = p64.forward(model_vis=v64, want_grad=True).item(), None
+    g64 = p64.adjoint()
+    x32 = p32.forward(mode=mode, model_vis=v32, want_grad=True).item()
+    g32 = p32.adjoint(mode=mode)
+    a, b = v32.cpu().numpy().astype(np.complex128), v64.cpu().numpy()
+    # the outputs are residual-free model visibilities (vis_output='model')
+    out = {'vis_rel_norm': float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+           'vis_rel_max': float(np.max(np.abs(a - b)) / np.max(np.abs(b))),
+           'chi2_rel': abs(x32 - x64) / abs(x64)}
+    for k in ('lm', 'stokes', 'G_term'):
+        ga, gb = g32[k].cpu().numpy().astype(np.complex128), g64[k].cpu().numpy()
+        out['grad_%s_rel_norm' % k] = float(np.linalg.norm(ga - gb) / np.linalg.norm(gb))
+    out['sample'] = '2 time steps x 3 channels, all %d sources and %d antennas' % (prob.nsrc, prob.na)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# timing
+# ---------------------------------------------------------------------------
+def time_resident(prob, mode, steps, warmup, ws):
+    """Device-resident chi^2 + gradient; returns (ms/step, fwd ms, adj ms)."""
+    import torch
+    stream = torch.cuda.current_stream()
+    grads = prob.empty_grads()
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        prob.forward(mode=mode, want_grad=True)
+        if ev:
+            ev[1].record(stream)
+        prob.adjoint(mode=mode, grads=grads)
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    for i in range(steps):
+        step(evs[i])
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    total = evs[0][0].elapsed_time(evs[-1][2])
+    fwd = [e[0].elapsed_time(e[1]) for e in evs]
+    adj = [e[1].elapsed_time(e[2]) for e in evs]
+    return total / steps, statistics.mean(fwd), statistics.mean(adj)
+
+
+def time_e2e(prob, mode, steps, warmup, ws):
+    """Through the public API with host buffers: per step the inputs are
+    copied from pinned host memory and chi^2 + gradients are copied back."""
+    import torch
+    names = ['observed_vis', 'flag', 'G_term', 'lm', 'stokes', 'alpha', 'gauss_shape', 'sersic_shape']
+    host = {n: prob.arrays[n].cpu().pin_memory() for n in names}
+    grads = prob.empty_grads()
+    ghost = {n: torch.empty(g.shape, dtype=g.dtype).pin_memory() for n, g in grads.items()}
+    x2host = torch.empty(1, dtype=torch.float64).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    d2h = 8 + sum(t.numel() * t.element_size() for t in ghost.values())
+
+    def step():
+        for n in names:
+            prob.arrays[n].copy_(host[n], non_blocking=True)
+        x2 = prob.forward(mode=mode, want_grad=True)
+        prob.adjoint(mode=mode, grads=grads)
+        x2host.copy_(x2, non_blocking=True)
+        for n in grads:
+            ghost[n].copy_(grads[n], non_blocking=True)
+
+    for _ in range(max(1, warmup)):
+        step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(steps):
+        step()
+    e.record()
+    torch.cuda.synchronize()
+    barrier(ws)
+    return s.elapsed_time(e) / steps, h2d, d2h
+
+
+def cpu_baseline(P, prob, max_units=None):
+    """The FP64 oracle (forward + gradient) on the host cores over a bounded
+    sample: (time, channel) units with all antennas and 2000 sources."""
+    from oracle import cpu_baseline as C
+    cores = os.cpu_count() or 1
+    nunits = max_units or 2 * cores
+    nsample = min(2000, prob.nsrc)
+    units = [((7 * i) % prob.ntime, (13 * i) % prob.nchan) for i in range(nunits)]
+    obs = prob.arrays['observed_vis']
+    probs = C.make_units(P, lambda t, ch: obs[t, :, ch].cpu().numpy(), units, nsample)
+    wall, procs = C.time_units(probs, cores)
+    terms = nunits * nsample * prob.nbl
+    return {'value': terms / wall, 'unit': UNIT, 'cores': procs, 'kind': 'port',
+            'sample': '%d (time, channel) units x %d sources x %d baselines, FP64 NumPy chi^2 + gradient, '
+                      '%.1f s wall' % (nunits, nsample, prob.nbl, wall)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            m = json.load(f)
+        return m['bf16_tflops'], m['bf16_tflops_sustained'], m['hbm_gbs'], 'measured'
+    except (OSError, KeyError, ValueError):
+        return 1900.0, 1700.0, 6800.0, 'fallback'
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's v4 path
+    (FP64 NumPy, forward + gradient) on the host cores, same workload."""
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    import numpy as np
+    from montblanc_gb300 import synth
+    from oracle import cpu_baseline as C
+    from oracle import rime_v4 as O
+    spec = synth.WORKLOADS[args.workload]
+    P = synth.make_problem(**spec, seed=args.seed, vis_arrays=False)
+    cores = os.cpu_count() or 1
+    nsample = min(2000, spec['npsrc'] + spec['ngsrc'] + spec['nssrc'])
+    nbl = P['antenna1'].shape[1]
+    rng = np.random.default_rng(args.seed)
+    times = []
+    for step in range(args.warmup + args.steps):
+        units = [(int(rng.integers(P['uvw'].shape[0])), int(rng.integers(P['frequency'].shape[0])))
+                 for _ in range(cores)]
+        probs = C.make_units(P, lambda t, ch: rng.normal(0, 0.1, (nbl, 4)) + 0j, units, nsample)
+        wall, procs = C.time_units(probs, cores)
+        if step >= args.warmup:
+            times.append(wall)
+    terms = cores * nsample * nbl
+    value = terms / statistics.mean(times)
+    line = {'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': args.gpus,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * statistics.mean(times),
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic',
+            'config': {'workload': workload_desc(args.workload), 'form': 'CPU FP64 (reference algorithm)'},
+            'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': procs, 'kind': 'port',
+                             'sample': 'per step %d (time, channel) units x %d sources x %d baselines'
+                                       % (cores, nsample, nbl)},
+            'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        return run_reference(args)
+    import torch
+    ws, rank, local = dist_init(args.gpus)
+    P, prob = build_workload(args.workload, args.seed + rank)
+    terms = terms_of(args.workload)
+
+    clocks = Clocks()
+    clocks.start()
+    ms, fwd_ms, adj_ms = time_resident(prob, args.mode, args.steps, args.warmup, ws)
+    clk = clocks.stop()
+    ms_max = max_over_ranks(ws, ms)
+    value = ws * terms / (ms_max * 1e-3)
+
+    plain = None
+    if args.compare_plain and args.mode != 'native':
+        pms, _, _ = time_resident(prob, 'native', args.steps, 1, ws)
+        pms = max_over_ranks(ws, pms)
+        plain = {'value': ws * terms / (pms * 1e-3), 'ms_per_step': pms, 'mode': 'native'}
+
+    e2e = None
+    if not args.no_e2e:
+        ems, h2d, d2h = time_e2e(prob, args.mode, args.steps, 1, ws)
+        ems = max_over_ranks(ws, ems)
+        e2e = {'value': ws * terms / (ems * 1e-3), 'unit': UNIT, 'h2d_bytes_per_step': h2d,
+               'd2h_bytes_per_step': d2h, 'ms_per_step': ems}
+
+    if rank != 0:
+        return
+    errs = errors_vs_fp64(P, prob, args.mode)
+    burst, sustained, hbm, src = peaks()
+    dominant = 'coh_adj_kernel' if adj_ms >= fwd_ms else 'coh_fwd_kernel'
+    dom_ms = max(adj_ms, fwd_ms)
+    dom_flops = (FLOPS_ADJ if dominant == 'coh_adj_kernel' else FLOPS_FWD) * terms
+    achieved = dom_flops / (dom_ms * 1e-3) / 1e12
+    sm_mhz = clk.get('sm_mhz') or 2070.0
+    fp32_peak = SM_COUNT * 128 * 2 * sm_mhz * 1e6 / 1e12
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms_max, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32' if args.mode == 'native' else 'f32 (%s products)' % args.mode,
+        'data': 'synthetic (seeded generator; observed = model + N(0,0.1) noise)',
+        'config': {'workload': workload_desc(args.workload), 'mode': args.mode, 'terms_per_step': terms,
+                   'l2': 'inputs larger than L2 (observed_vis alone %.1f GB)'
+                         % (prob.arrays['observed_vis'].numel() * 8 / 1e9),
+                   'phase': 'FP64 argument and range reduction', 'replicas': ws},
+        'forward_ms': fwd_ms, 'adjoint_ms': adj_ms,
+        'roofline': {'bound': 'tensor', 'kernel': dominant, 'achieved': achieved, 'peak': sustained,
+                     'unit': 'TFLOP/s', 'frac': achieved / sustained,
+                     'peak_source': '%s bf16 sustained (MEASURED_PEAKS.json)' % src,
+                     'traffic': NCU_TRAFFIC.get((dominant, args.workload)),
+                     'algorithmic_flops_per_launch': dom_flops,
+                     'fp32_simt_peak_tflops_at_clock': fp32_peak,
+                     'fp32_simt_frac': achieved / fp32_peak},
+        'errors_vs_fp64': errs,
+        'gpu_launches': 5 * args.steps + (args.steps if args.mode != 'native' else 0),
+        'clocks': clk,
+    }
+    if plain:
+        line['plain_fp32'] = plain
+    if e2e:
+        line['e2e'] = e2e
+    if not args.no_cpu:
+        line['cpu_baseline'] = cpu_baseline(P, prob)
+    print(json.dumps(line))
+
+
+if __name__ == '__main__':
+    main()

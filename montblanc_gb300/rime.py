@@ -50,13 +50,26 @@ class RimeProblem(object):
         tft = torch.float64 if dtype == 'double' else torch.float32
         tct = torch.complex128 if dtype == 'double' else torch.complex64
         arrays = {}
+        ntime, nbl, nchan = P['antenna1'].shape[0], P['antenna1'].shape[1], P['frequency'].shape[0]
+        vshape = (ntime, nbl, nchan, 4)
         for k in FLOAT_INPUTS:
+            if k == 'weight_vector' and k not in P:
+                # only read when weights are applied
+                arrays[k] = (torch.ones(vshape, dtype=tft, device=device)
+                             if P.get('use_weight_vector', False) else None)
+                continue
             arrays[k] = torch.as_tensor(np.ascontiguousarray(P[k])).to(device=device, dtype=tft)
         for k in COMPLEX_INPUTS:
+            if k == 'observed_vis' and k not in P:
+                arrays[k] = torch.zeros(vshape, dtype=tct, device=device)
+                continue
             arrays[k] = torch.as_tensor(np.ascontiguousarray(P[k])).to(device=device, dtype=tct)
         arrays['antenna1'] = torch.as_tensor(np.ascontiguousarray(P['antenna1'], dtype=np.int32)).to(device)
         arrays['antenna2'] = torch.as_tensor(np.ascontiguousarray(P['antenna2'], dtype=np.int32)).to(device)
-        arrays['flag'] = torch.as_tensor(np.ascontiguousarray(P['flag'], dtype=np.uint8)).to(device)
+        if 'flag' in P:
+            arrays['flag'] = torch.as_tensor(np.ascontiguousarray(P['flag'], dtype=np.uint8)).to(device)
+        else:
+            arrays['flag'] = torch.zeros(vshape, dtype=torch.uint8, device=device)
         props = {k: float(P[k]) for k in _cabi.PROP_NAMES}
         return cls(arrays, props, P['npsrc'], P['ngsrc'], P['nssrc'], P.get('use_weight_vector', False),
                    P.get('residuals', False), dtype=dtype, device=device)

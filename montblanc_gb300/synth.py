@@ -85,8 +85,12 @@ def beam_cube(rng, lw=50, mh=50, nud=32, props=DEFAULT_PROPS):
 def make_problem(ntime, na, nchan, npsrc, ngsrc=0, nssrc=0, seed=0,
                  beam_shape=(50, 50, 32), use_weight_vector=False,
                  residuals=False, random_weights=False, flag_fraction=0.0,
-                 antenna_scaling_noise=0.0, auto_correlations=False):
-    """Return a problem dict of float64/complex128 NumPy arrays."""
+                 antenna_scaling_noise=0.0, auto_correlations=False, vis_arrays=True):
+    """Return a problem dict of float64/complex128 NumPy arrays.
+
+    With ``vis_arrays=False`` the visibility-sized arrays (flag,
+    weight_vector, observed_vis) are left out, for callers that create them
+    on the device."""
     rng = np.random.default_rng(seed)
     nsrc = npsrc + ngsrc + nssrc
     nbl = nr_of_baselines(na, auto_correlations)
@@ -123,6 +127,8 @@ def make_problem(ntime, na, nchan, npsrc, ngsrc=0, nssrc=0, seed=0,
                                   rng.uniform(-0.3, 0.3, nssrc),
                                   rng.uniform(1e-5, 1e-4, nssrc)])
     vshape = (ntime, nbl, nchan, 4)
+    if not vis_arrays:
+        return P
     P['flag'] = (rng.random(vshape) < flag_fraction).astype(np.uint8)
     P['weight_vector'] = rng.random(vshape) if random_weights else np.ones(vshape)
     P['observed_vis'] = np.zeros(vshape, dtype=np.complex128)

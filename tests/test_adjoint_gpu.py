@@ -12,13 +12,22 @@ pytestmark = pytest.mark.gpu
 PARAMS = ('lm', 'stokes', 'alpha', 'gauss_shape', 'sersic_shape', 'G_term')
 
 
-def small_problem(seed, use_w, residuals=False, na=6, np_=4, ng=3, ns=2):
+def small_problem(seed, use_w, residuals=False, na=6, np_=4, ng=3, ns=2, offset=0.0):
+    """Observed = model + noise; with ``offset`` > 0 the gradient is then
+    evaluated at source positions displaced by N(0, offset) from the truth.
+
+    At the truth the gradient is a noise-level quantity, and the ~1e-6
+    relative FP32 error of the model biases it by about sqrt(N) dM / sigma
+    (~1e-3 relative here); FP32 gradients are therefore checked away from
+    the optimum, where their relative error is meaningful."""
     P = synth.make_problem(ntime=3, na=na, nchan=5, npsrc=np_, ngsrc=ng, nssrc=ns, seed=seed,
                            beam_shape=(12, 12, 6), random_weights=True, flag_fraction=0.15,
                            antenna_scaling_noise=0.05, use_weight_vector=use_w, residuals=residuals)
     model, _, _ = O.forward(P)
     synth.add_noise(P, model, sigma=0.5, seed=seed + 1)
     P['sigma_sqrd'] = 0.7
+    if offset:
+        P['lm'] = P['lm'] + np.random.default_rng(seed + 2).normal(0.0, offset, P['lm'].shape)
     return P
 
 
@@ -31,7 +40,7 @@ def grad_err(g, ref):
 @pytest.mark.parametrize('seed,use_w,resid', [(21, True, False), (22, False, False), (23, True, True)])
 def test_adjoint_matches_numpy_gradient(dtype, tol, seed, use_w, resid):
     from montblanc_gb300.rime import RimeProblem
-    P = small_problem(seed, use_w, resid)
+    P = small_problem(seed, use_w, resid, offset=0.0 if dtype == 'double' else 2e-4)
     chi2, ref = OA.chi2_grad(P)
     prob = RimeProblem.from_numpy(P, dtype=dtype)
     x2, g = prob.chi2_and_grad()
@@ -85,7 +94,7 @@ def test_gradient_finite_differences_medium_workload():
     rng = np.random.default_rng(7)
     names = ['lm'] * 10 + ['stokes'] * 10 + ['alpha'] * 8 + ['gauss_shape'] * 8 + ['sersic_shape'] * 6 + \
             ['G_term'] * 8
-    worst = 0.0
+    checked = 0
     for name in names:
         arr = prob.arrays[name]
         idx = tuple(int(rng.integers(0, n)) for n in arr.shape)
@@ -102,6 +111,9 @@ def test_gradient_finite_differences_medium_workload():
         num = (fp - fm) / (2 * h)
         an = g[name][idx].item()
         an = an.imag if imag else (an.real if isinstance(an, complex) else an)
-        err = abs(an - num) / max(abs(num), 1e-6 * abs(x2.item()))
-        worst = max(worst, err)
-        assert err < 1e-4, (name, idx, an, num)
+        # rounding floor of a central difference of a chi^2 of this size
+        fd_noise = 8 * np.finfo(np.float64).eps * abs(x2.item()) / h
+        assert abs(an - num) <= 1e-4 * abs(num) + fd_noise, (name, idx, an, num, fd_noise)
+        checked += abs(num) > 10 * fd_noise
+    # most of the 50 draws must be far enough above the FD floor to count
+    assert checked >= 25, checked
