@@ -217,6 +217,35 @@ mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
                           const mb_rime_grads* grads, void* workspace,
                           size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Allocation-free forward.  No counterpart in the reference.
+ *
+ * For callers that must not allocate device memory themselves: applications
+ * that hand all device memory to their own pool or framework allocator at
+ * start-up (so a foreign cudaMalloc fails or breaks their budget), and
+ * latency-bound pipelines that cannot afford cudaMalloc/cudaFree, which may
+ * synchronise the device.  Such callers cannot size and pass the workspace
+ * mb_rime_forward needs.
+ *
+ * Same inputs, outputs and results as mb_rime_forward in MB_MODE_NATIVE
+ * with want_grad = 0.  Its only scratch (one FP64 partial sum per (time,
+ * channel) unit) is a static device array inside the library: at most
+ * mb_rime_noalloc_max_units() = 131072 units (ntime * nchan active
+ * extents); larger requests return MB_ERR_UNSUPPORTED.  The array costs
+ * 1 MiB on every GPU that loads the library, for the life of the process.
+ * The first call on a device looks the array's device address up
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array: calls whose kernels may run at the same time
+ * (on unordered streams) race on it and must be serialised by the caller.
+ * It allocates nothing: no cudaMalloc, cudaFree or allocating library call.
+ * ---------------------------------------------------------------------- */
+size_t mb_rime_noalloc_max_units(void);
+mb_status mb_rime_forward_noalloc(mb_dtype dtype, const mb_dims* dims,
+                                  const mb_props* props, uint32_t options,
+                                  const mb_rime_inputs* in, void* model_vis,
+                                  void* chi_sqrd_result, double* X2,
+                                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif

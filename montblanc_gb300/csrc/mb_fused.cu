@@ -20,6 +20,7 @@
 // RimeSumCoherencies.py:103-393 (epilogue, source-batch semantics).  The
 // adjoint has no reference counterpart.
 #include <algorithm>
+#include <mutex>
 
 #include "mb_fused.h"
 
@@ -125,7 +126,15 @@ __device__ void load_sources(const FusedArgs<T>& A, int t, int ch, int s0, int n
 
 template <typename T>
 __device__ __forceinline__ Cx<T> phase_term(const FusedArgs<T>& A, int t, int s, int a, T f, double nu_over_c) {
-  double phi = A.phi[(size_t(t) * A.nsrc + s) * A.na + a];
+  double phi;
+  if (A.phi != nullptr) {
+    phi = A.phi[(size_t(t) * A.nsrc + s) * A.na + a];
+  } else {  // no table: the same FP64 path length, formed in place
+    double l = A.lm[2 * s], m = A.lm[2 * s + 1];
+    double n = sqrt(1.0 - l * l - m * m) - 1.0;
+    const T* p = A.uvw + 3 * (size_t(t) * A.lna + a);
+    phi = l * double(p[0]) + m * double(p[1]) + n * double(p[2]);
+  }
   if (sizeof(T) == 8) return phase_from_phi<T>(phi, double(f));
   return phase_from_cycles<T>(phi, nu_over_c);
 }
@@ -755,6 +764,10 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.sersic = (const T*)in->sersic_shape; A.weight = (const T*)in->weight_vector; A.obs = (const T*)in->observed_vis;
   A.ant1 = in->antenna1; A.ant2 = in->antenna2; A.flag = in->flag;
   A.model_vis = (T*)model_vis; A.chi2 = (T*)chi2;
+  A.Vpoint = nullptr;
+  A.phi = nullptr; A.partial = nullptr; A.gV = nullptr; A.dG = nullptr;
+  A.acc_lm = A.acc_stokes = A.acc_alpha = A.acc_gauss = A.acc_sersic = nullptr;
+  if (ws == nullptr) return MB_OK;
   char* w = static_cast<char*>(ws);
   A.phi = reinterpret_cast<const double*>(w + L.phi);
   A.partial = reinterpret_cast<double*>(w + L.partial);
@@ -765,7 +778,6 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.acc_alpha = reinterpret_cast<double*>(w + L.acc_alpha);
   A.acc_gauss = reinterpret_cast<double*>(w + L.acc_gauss);
   A.acc_sersic = reinterpret_cast<double*>(w + L.acc_sersic);
-  A.Vpoint = nullptr;
   return MB_OK;
 }
 
@@ -867,6 +879,66 @@ size_t fused_workspace_size(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool
   return ws_layout(dtype, mode, d, want_grad).total;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free forward (mb_rime_forward_noalloc)
+// ---------------------------------------------------------------------------
+// Its only scratch, one FP64 chi^2 partial per (time, channel) unit, lives in
+// this file-scope device array.  Every GPU that loads the library holds the
+// array (1 MiB) until the process exits.  All calls share it: calls whose
+// kernels overlap on the GPU (different streams, no ordering between them)
+// race on it.  Every slot a call reads is written by the same call first, so
+// nothing needs clearing between calls.
+constexpr size_t kNoallocMaxUnits = 131072;
+static __device__ __align__(256) double g_noalloc_partials[kNoallocMaxUnits];
+
+constexpr int kMaxDevices = 256;
+static std::mutex g_noalloc_mutex;
+static double* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_partials on the current device.  In host code
+// the symbol names a host-side stand-in, so the address is looked up with
+// cudaGetSymbolAddress once per device (with that device current) and cached.
+mb_status noalloc_scratch(double** out) {
+  int dev = 0;
+  MB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(MB_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess)
+      return fail(MB_ERR_CUDA, "cudaGetSymbolAddress(g_noalloc_partials): %s", cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return MB_OK;
+}
+
+namespace {
+template <typename T>
+mb_status launch_forward_noalloc(FusedArgs<T> A, double* partials, double* X2, cudaStream_t stream) {
+  A.phi = nullptr;  // path lengths formed in the kernel instead of a table
+  A.partial = partials;
+  A.want_grad = false;
+  const int units = A.ntime * A.nchan;
+  if (units == 0) {
+    sum_partials_kernel<<<1, 1024, 0, stream>>>(partials, 0, 1.0, X2);
+    return check_launch("sum_partials_kernel");
+  }
+  constexpr int RP = FwdTile<T>::RP, RQ = FwdTile<T>::RQ;
+  SmemPlan S = make_plan<T>(A.na, false);
+  if (S.total > 227 * 1024)
+    return fail(MB_ERR_UNSUPPORTED, "fused forward needs %zu bytes of shared memory for na=%d (max 232448)",
+                S.total, A.na);
+  auto kern = coh_fwd_kernel<T, RP, RQ>;
+  MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
+  kern<<<units, kFusedThreads, S.total, stream>>>(A, S);
+  MB_CHECK(check_launch("coh_fwd_kernel"));
+  sum_partials_kernel<<<1, 1024, 0, stream>>>(partials, units, A.weights ? 1.0 : A.inv_sigma2, X2);
+  return check_launch("sum_partials_kernel");
+}
+}  // namespace
+
 }  // namespace mb
 
 using namespace mb;
@@ -927,6 +999,38 @@ mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims, con
   FusedArgs<double> A;
   fill_args(A, dims, props, options, in, nullptr, nullptr, true, workspace, L);
   return launch_adjoint(A, grad_scale, grads, workspace, L, s);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+size_t mb_rime_noalloc_max_units(void) { return kNoallocMaxUnits; }
+
+mb_status mb_rime_forward_noalloc(mb_dtype dtype, const mb_dims* dims, const mb_props* props, uint32_t options,
+                                  const mb_rime_inputs* in, void* model_vis, void* chi_sqrd_result, double* X2,
+                                  void* stream) {
+  MB_CHECK(check_inputs(dims, props, options, in, model_vis));
+  MB_REQUIRE(X2, "X2");
+  if (dtype != MB_FLOAT32 && dtype != MB_FLOAT64) return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
+  const size_t units = size_t(ext(dims->ntime)) * ext(dims->nchan);
+  if (units > kNoallocMaxUnits)
+    return fail(MB_ERR_UNSUPPORTED,
+                "mb_rime_forward_noalloc handles at most %zu (time, channel) units (got %zu = %u x %u); "
+                "split the call over time or use mb_rime_forward with a workspace",
+                kNoallocMaxUnits, units, ext(dims->ntime), ext(dims->nchan));
+  double* partials = nullptr;
+  MB_CHECK(noalloc_scratch(&partials));
+  cudaStream_t s = as_stream(stream);
+  WsLayout L = ws_layout(dtype, MB_MODE_NATIVE, dims, false);
+  if (dtype == MB_FLOAT32) {
+    FusedArgs<float> A;
+    fill_args(A, dims, props, options, in, model_vis, chi_sqrd_result, false, nullptr, L);
+    return launch_forward_noalloc(A, partials, X2, s);
+  }
+  FusedArgs<double> A;
+  fill_args(A, dims, props, options, in, model_vis, chi_sqrd_result, false, nullptr, L);
+  return launch_forward_noalloc(A, partials, X2, s);
 }
 
 }  // extern "C"
