@@ -217,6 +217,14 @@ mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
                           const mb_rime_grads* grads, void* workspace,
                           size_t workspace_bytes, void* stream);
 
+/* Diagnostic, no counterpart in the reference: D (128 x 128, row-major) =
+ * A (128 x K) . B (128 x K)^T for row-major FP32 device arrays, computed
+ * with the split-precision tensor-core operand path of the fused kernels
+ * (mode MB_MODE_SPLIT_TF32: K % 32 == 0; MB_MODE_SPLIT_BF16: K % 64 == 0).
+ * *status (device int) is set to 1 if a bounded wait gave up. */
+mb_status mb_tc_selftest(const float* A, const float* B, int K, int mode,
+                         float* D, int* status, void* stream);
+
 /* ------------------------------------------------------------------------
  * Allocation-free forward.  No counterpart in the reference.
  *

@@ -20,16 +20,17 @@
 // RimeSumCoherencies.py:103-393 (epilogue, source-batch semantics).  The
 // adjoint has no reference counterpart.
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 
 #include "mb_fused.h"
+#include "mb_tc_layout.cuh"
+#include "mb_tcgen05.cuh"
 
 namespace mb {
 
 __global__ void sum_partials_kernel(const double* __restrict__ partial, int n, double scale,
                                     double* __restrict__ out);
-mb_status tc_point_coherencies(const FusedArgs<float>& A, mb_mode mode, float* Vpoint, cudaStream_t stream);
-size_t tc_scratch_bytes(const mb_dims* d);
 
 namespace {
 
@@ -37,7 +38,7 @@ template <typename T> struct FwdTile;
 template <> struct FwdTile<float> { static constexpr int RP = 2, RQ = 4, ST = 16; };
 template <> struct FwdTile<double> { static constexpr int RP = 1, RQ = 2, ST = 8; };
 template <typename T> struct AdjTile;
-template <> struct AdjTile<float> { static constexpr int RA = 2, RS = 4, ST = 16; };
+template <> struct AdjTile<float> { static constexpr int RA = 2, RS = 4, ST = 32; };
 template <> struct AdjTile<double> { static constexpr int RA = 1, RS = 2, ST = 8; };
 
 constexpr int kNAcc = 10;  // l, m, I, Q, U, V, alpha, shape0, shape1, shape2
@@ -55,14 +56,27 @@ SmemPlan make_plan(int na, bool adjoint) {
   S.st = adjoint ? AdjTile<T>::ST : FwdTile<T>::ST;
   S.npairs = na * (na + 1) / 2;
   S.nitems = count_pair_tiles(na, FwdTile<T>::RP, FwdTile<T>::RQ);
+  if (adjoint) {
+    S.nthreads = kFusedThreads;
+    S.groups = 1;
+  } else if (S.nitems <= kFwdMaxThreads) {
+    // one pair tile per thread; spare threads split each tile's sources
+    S.nthreads = std::max(128, (S.nitems + 31) / 32 * 32);
+    S.groups = std::min(8, std::max(1, S.nthreads / S.nitems));
+  } else {
+    S.nthreads = kFusedThreads;
+    S.groups = 1;
+  }
   size_t o = 0;
   auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 16); return r; };
   S.off_ant = take(sizeof(AntInfo<T>) * na);
-  S.off_antd = take(sizeof(double) * 3 * na);
+  S.off_antd = take(0);
   S.off_src = take(sizeof(SrcInfo<T>) * S.st);
   S.off_J = take(sizeof(Jones<T>) * S.st * S.nap);
   S.off_gJ = take(adjoint ? sizeof(Jones<T>) * S.st * S.nap : 0);
   S.off_V = take(sizeof(Jones<T>) * S.npairs);
+  // FP32 forward: low parts of float-float pair accumulators
+  S.off_Vlo = take(!adjoint && sizeof(T) == 4 ? sizeof(Jones<T>) * S.npairs : 0);
   S.off_items = take(adjoint ? 0 : sizeof(int) * (S.nitems + 128));
   S.off_acc = take(adjoint ? sizeof(T) * S.st * kNAcc : 0);
   S.off_red = take(sizeof(double) * 32);
@@ -74,7 +88,7 @@ SmemPlan make_plan(int na, bool adjoint) {
 // Shared set-up and producer
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ void load_antennas(const FusedArgs<T>& A, int t, int ch, AntInfo<T>* sa, double* sad) {
+__device__ void load_antennas(const FusedArgs<T>& A, int t, int ch, AntInfo<T>* sa) {
   for (int a = threadIdx.x; a < A.na; a += blockDim.x) {
     size_t ta = size_t(t) * A.lna + a;
     AntInfo<T> ai;
@@ -87,9 +101,8 @@ __device__ void load_antennas(const FusedArgs<T>& A, int t, int ch, AntInfo<T>* 
     ai.pe_l = A.pe[2 * tac]; ai.pe_m = A.pe[2 * tac + 1];
     size_t ac = size_t(a) * A.lchan + ch;
     ai.sc_l = A.sc[2 * ac]; ai.sc_m = A.sc[2 * ac + 1];
-    ai.u = A.uvw[3 * ta]; ai.v = A.uvw[3 * ta + 1];
+    ai.u = A.uvw[3 * ta]; ai.v = A.uvw[3 * ta + 1]; ai.w = A.uvw[3 * ta + 2];
     sa[a] = ai;
-    if (sad) { sad[3 * a] = A.uvw[3 * ta]; sad[3 * a + 1] = A.uvw[3 * ta + 1]; sad[3 * a + 2] = A.uvw[3 * ta + 2]; }
   }
 }
 
@@ -106,6 +119,11 @@ __device__ void load_sources(const FusedArgs<T>& A, int t, int ch, int s0, int n
     int s = s0 + i;
     SrcInfo<T> si;
     si.l = A.lm[2 * s]; si.m = A.lm[2 * s + 1];
+    {
+      const double l = si.l, m = si.m, nf = sqrt(1.0 - l * l - m * m);
+      si.l_over_n = T(l / nf);
+      si.m_over_n = T(m / nf);
+    }
     size_t st = size_t(s) * A.ltime + t;
     si.I = A.stokes[4 * st]; si.Q = A.stokes[4 * st + 1];
     si.U = A.stokes[4 * st + 2]; si.V = A.stokes[4 * st + 3];
@@ -139,29 +157,31 @@ __device__ __forceinline__ Cx<T> phase_term(const FusedArgs<T>& A, int t, int s,
   return phase_from_cycles<T>(phi, nu_over_c);
 }
 
+// J(s, a) = E(s, a) . (K(s, a) sqrt(B)(s)) for one source and antenna.
+template <typename T>
+__device__ __forceinline__ Jones<T> compute_jones(const FusedArgs<T>& A, int t, int s, int a, const SrcInfo<T>& src,
+                                                  const AntInfo<T>& ai, T f, double nu_over_c,
+                                                  const ChanPos<T>& cp) {
+  const BeamGeom G{A.lw, A.mh, A.nud};
+  Cx<T> K = phase_term(A, t, s, a, f, nu_over_c);
+  T l, m;
+  beam_lm<T>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
+  GridPos<T> gl = grid_pos<T>(l, A.ll, A.ul, A.lscale, A.lw);
+  GridPos<T> gm = grid_pos<T>(m, A.lmm, A.um, A.mscale, A.mh);
+  Jones<T> E = beam_interp<T>(A.E_beam, G, gl, gm, cp);
+  Jones<T> KB = {cmul(K, src.B.a), cmul(K, src.B.b), cmul(K, src.B.c), cmul(K, src.B.d)};
+  return jmul(E, KB);
+}
+
 // J(s, a) for the tile into sJ[si * nap + a]; padded antennas get zeros.
 template <typename T>
 __device__ void produce_jones(const FusedArgs<T>& A, const SmemPlan& S, int t, int ch, int s0, int ns,
                               const SrcInfo<T>* ss, const AntInfo<T>* sa, Jones<T>* sJ, const ChanPos<T>& cp) {
   const T f = A.freq[ch];
   const double nu_over_c = double(f) / kLightSpeed;
-  const BeamGeom G{A.lw, A.mh, A.nud};
   for (int i = threadIdx.x; i < ns * S.nap; i += blockDim.x) {
     int si = i / S.nap, a = i - si * S.nap;
-    Jones<T> J = jzero<T>();
-    if (a < A.na) {
-      const SrcInfo<T>& src = ss[si];
-      Cx<T> K = phase_term(A, t, s0 + si, a, f, nu_over_c);
-      const AntInfo<T>& ai = sa[a];
-      T l, m;
-      beam_lm<T>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
-      GridPos<T> gl = grid_pos<T>(l, A.ll, A.ul, A.lscale, A.lw);
-      GridPos<T> gm = grid_pos<T>(m, A.lmm, A.um, A.mscale, A.mh);
-      Jones<T> E = beam_interp<T>(A.E_beam, G, gl, gm, cp);
-      Jones<T> KB = {cmul(K, src.B.a), cmul(K, src.B.b), cmul(K, src.B.c), cmul(K, src.B.d)};
-      J = jmul(E, KB);
-    }
-    sJ[i] = J;
+    sJ[i] = a < A.na ? compute_jones(A, t, s0 + si, a, ss[si], sa[a], f, nu_over_c, cp) : jzero<T>();
   }
 }
 
@@ -269,87 +289,115 @@ __device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const J
 // ---------------------------------------------------------------------------
 // Forward
 // ---------------------------------------------------------------------------
+// Pair accumulators: FP64 in FP64 mode; float-float (hi + lo, TwoSum) in
+// FP32 mode, so that the sum over thousands of source tiles does not lose
+// the precision of FP32 (the per-tile partial sums are plain FP32).
+template <typename T>
+__device__ __forceinline__ void fold_pair(Jones<T>* sV, Jones<T>* sVlo, int idx, const Jones<T>& x) {
+  T* hi = reinterpret_cast<T*>(sV + idx);
+  const T* xv = reinterpret_cast<const T*>(&x);
+  if (sVlo == nullptr) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) hi[k] += xv[k];
+    return;
+  }
+  T* lo = reinterpret_cast<T*>(sVlo + idx);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    T a = hi[k], b = xv[k];
+    T sum = a + b;
+    T bp = sum - a;
+    T err = (a - (sum - bp)) + (b - bp);
+    hi[k] = sum;
+    lo[k] += err;
+  }
+}
+
+// Accumulate the tile's sources into the pair matrix.  Work item k covers
+// pair tile (k mod nitems) for the sources si = g, g + G, ... of the tile,
+// g = k / nitems, G = S.groups.  With G > 1 every thread owns at most one
+// item and the groups fold their partial sums one after the other.
 template <typename T, int RP, int RQ>
 __device__ void consume_pairs(const FusedArgs<T>& A, const SmemPlan& S, int ns, const SrcInfo<T>* ss,
-                              const AntInfo<T>* sa, const Jones<T>* sJ, Jones<T>* sV, const int* items,
-                              bool extended, T kg, T ks) {
-  for (int k = threadIdx.x; k < S.nitems; k += blockDim.x) {
-    int it = items[k];
-    int p0 = (it & 0xffff) * RP, q0 = (it >> 16) * RQ;
+                              const AntInfo<T>* sa, const Jones<T>* sJ, Jones<T>* sV, Jones<T>* sVlo,
+                              const int* items, bool extended, T kg, T ks) {
+  const int total = S.nitems * S.groups;
+  const int rounds = (total + blockDim.x - 1) / blockDim.x;
+  for (int round = 0; round < rounds; ++round) {
+    const int k = round * blockDim.x + threadIdx.x;
+    const bool active = k < total;
+    const int item = active ? k % S.nitems : 0, g = active ? k / S.nitems : 0;
+    const int it = items[item];
+    const int p0 = (it & 0xffff) * RP, q0 = (it >> 16) * RQ;
     Jones<T> acc[RP][RQ];
     T u[RP][RQ], v[RP][RQ];
 #pragma unroll
     for (int r = 0; r < RP; ++r)
 #pragma unroll
       for (int c = 0; c < RQ; ++c) {
-        int p = p0 + r, q = q0 + c;
-        bool ok = p <= q && q < A.na;
-        acc[r][c] = ok ? sV[pair_index(p, q, A.na)] : jzero<T>();
+        acc[r][c] = jzero<T>();
         if (extended) {
-          int pp = min(p, A.na - 1), qq = min(q, A.na - 1);
+          int pp = min(p0 + r, A.na - 1), qq = min(q0 + c, A.na - 1);
           u[r][c] = sa[qq].u - sa[pp].u;
           v[r][c] = sa[qq].v - sa[pp].v;
         }
       }
-    for (int si = 0; si < ns; ++si) {
-      Jones<T> Ja[RP], Jb[RQ];
+    if (active) {
+      for (int si = g; si < ns; si += S.groups) {
+        Jones<T> Ja[RP], Jb[RQ];
 #pragma unroll
-      for (int r = 0; r < RP; ++r) Ja[r] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + p0 + r));
+        for (int r = 0; r < RP; ++r) Ja[r] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + p0 + r));
 #pragma unroll
-      for (int c = 0; c < RQ; ++c) Jb[c] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + q0 + c));
-      if (!extended) {
+        for (int c = 0; c < RQ; ++c) Jb[c] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + q0 + c));
+        if (!extended) {
 #pragma unroll
-        for (int r = 0; r < RP; ++r)
+          for (int r = 0; r < RP; ++r)
 #pragma unroll
-          for (int c = 0; c < RQ; ++c) jmac_h(acc[r][c], Ja[r], Jb[c]);
-      } else {
-        const SrcInfo<T>& src = ss[si];
+            for (int c = 0; c < RQ; ++c) jmac_h(acc[r][c], Ja[r], Jb[c]);
+        } else {
+          const SrcInfo<T>& src = ss[si];
+#pragma unroll
+          for (int r = 0; r < RP; ++r)
+#pragma unroll
+            for (int c = 0; c < RQ; ++c) {
+              T sh = shape_factor<T>(src.type, u[r][c], v[r][c], src.s0, src.s1, src.s2, kg, ks);
+              jmac_h(acc[r][c], jscale(Ja[r], sh), Jb[c]);
+            }
+        }
+      }
+    }
+    for (int gg = 0; gg < S.groups; ++gg) {
+      if (S.groups > 1) __syncthreads();
+      if (active && g == gg) {
 #pragma unroll
         for (int r = 0; r < RP; ++r)
 #pragma unroll
           for (int c = 0; c < RQ; ++c) {
-            T sh = shape_factor<T>(src.type, u[r][c], v[r][c], src.s0, src.s1, src.s2, kg, ks);
-            jmac_h(acc[r][c], jscale(Ja[r], sh), Jb[c]);
+            int p = p0 + r, q = q0 + c;
+            if (p <= q && q < A.na) fold_pair(sV, sVlo, pair_index(p, q, A.na), acc[r][c]);
           }
       }
     }
-#pragma unroll
-    for (int r = 0; r < RP; ++r)
-#pragma unroll
-      for (int c = 0; c < RQ; ++c) {
-        int p = p0 + r, q = q0 + c;
-        if (p <= q && q < A.na) sV[pair_index(p, q, A.na)] = acc[r][c];
-      }
   }
 }
 
 template <typename T, int RP, int RQ>
-__global__ void __launch_bounds__(kFusedThreads) coh_fwd_kernel(FusedArgs<T> A, SmemPlan S) {
+__global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A, SmemPlan S) {
   extern __shared__ __align__(16) unsigned char smem[];
   AntInfo<T>* sa = reinterpret_cast<AntInfo<T>*>(smem + S.off_ant);
   SrcInfo<T>* ss = reinterpret_cast<SrcInfo<T>*>(smem + S.off_src);
   Jones<T>* sJ = reinterpret_cast<Jones<T>*>(smem + S.off_J);
   Jones<T>* sV = reinterpret_cast<Jones<T>*>(smem + S.off_V);
+  Jones<T>* sVlo = sizeof(T) == 4 ? reinterpret_cast<Jones<T>*>(smem + S.off_Vlo) : nullptr;
   int* items = reinterpret_cast<int*>(smem + S.off_items);
   double* red = reinterpret_cast<double*>(smem + S.off_red);
 
   const int unit = blockIdx.x;
   const int t = unit / A.nchan, ch = unit - t * A.nchan;
-  load_antennas(A, t, ch, sa, nullptr);
-  const bool have_point_tc = A.Vpoint != nullptr;
+  load_antennas(A, t, ch, sa);
   for (int i = threadIdx.x; i < S.npairs; i += blockDim.x) {
-    Jones<T> z = jzero<T>();
-    if (have_point_tc) {
-      // Point-source coherencies from the tensor-core kernel: packed
-      // (p, q) -> 4 complex, row-major over the full na x na matrix.
-      int p = 0, rem = i;
-      while (rem >= A.na - p) { rem -= A.na - p; ++p; }
-      int q = p + rem;
-      const float* src = A.Vpoint + (size_t(unit) * A.na * A.na + size_t(p) * A.na + q) * 8;
-      z.a = {T(src[0]), T(src[1])}; z.b = {T(src[2]), T(src[3])};
-      z.c = {T(src[4]), T(src[5])}; z.d = {T(src[6]), T(src[7])};
-    }
-    sV[i] = z;
+    sV[i] = jzero<T>();
+    if (sVlo) sVlo[i] = jzero<T>();
   }
   if (threadIdx.x == 0) {
     const int npt = (A.na + RP - 1) / RP, nqt = (A.na + RQ - 1) / RQ;
@@ -362,19 +410,269 @@ __global__ void __launch_bounds__(kFusedThreads) coh_fwd_kernel(FusedArgs<T> A, 
   const T f = A.freq[ch];
   const ChanPos<T> cp = chan_pos<T>(f, A.lfreq, A.ufreq, A.nud);
   const T kg = A.gauss_scale * f, ks = A.two_pi_over_c * f;
-  const int sbeg = have_point_tc ? A.npsrc : 0;
-  for (int s0 = sbeg; s0 < A.nsrc;) {
+  for (int s0 = 0; s0 < A.nsrc;) {
     int s1 = s0 < A.npsrc ? min(s0 + S.st, A.npsrc) : min(s0 + S.st, A.nsrc);
     int ns = s1 - s0;
     load_sources(A, t, ch, s0, ns, ss);
     __syncthreads();
     produce_jones(A, S, t, ch, s0, ns, ss, sa, sJ, cp);
     __syncthreads();
-    consume_pairs<T, RP, RQ>(A, S, ns, ss, sa, sJ, sV, items, s0 >= A.npsrc, kg, ks);
+    consume_pairs<T, RP, RQ>(A, S, ns, ss, sa, sJ, sV, sVlo, items, s0 >= A.npsrc, kg, ks);
     __syncthreads();
     s0 = s1;
   }
+  if (sVlo) {  // collapse the float-float accumulators
+    for (int i = threadIdx.x; i < S.npairs; i += blockDim.x) sV[i] = jadd(sV[i], sVlo[i]);
+    __syncthreads();
+  }
   epilogue(A, t, ch, unit, sV, sJ, red);
+}
+
+// ---------------------------------------------------------------------------
+// Split-precision forward: point-source coherencies on the tensor cores
+// ---------------------------------------------------------------------------
+// Per (time, channel) unit, with A (128 x 4k) the per-stage operand whose row
+// r = 2a + i holds, for the stage's k sources s and Jones columns c,
+// Re J_s,a[i][c] (K index 2s + c) and Im J_s,a[i][c] (K index 2k + 2s + c):
+//   D_re = A A^T            = Re sum_s J_a J_b^H  (rows 2a+i, columns 2b+j)
+//   D_x  = A_im A_re^T,  Im sum_s J_a J_b^H = D_x - D_x^T,
+// with each operand value split into hi + lo parts and D += hi.hi + hi.lo +
+// lo.hi, FP32 accumulation in TMEM over kTcGroup stages, then folded into
+// float-float pair accumulators in shared memory (so the sum over all
+// sources keeps better than FP32 precision).
+constexpr int kTcProducers = 256;          // warps 0-7: operands, TMEM drain
+constexpr int kTcThreads = kTcProducers + 32;  // warp 8: MMA issue
+constexpr int kTcStages = 2;
+constexpr int kTcGroup = 16;               // stages per TMEM accumulation group
+constexpr uint32_t kTcCols = 256;          // D_re: columns 0-127, D_x: 128-255
+
+struct TcPlan {
+  size_t off_stage, off_bar, total;
+  int group;
+};
+
+__device__ __forceinline__ void named_sync_producers() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kTcProducers) : "memory");
+}
+
+// Barrier over the producer warps that also ORs a predicate across them, so
+// that every producer takes the same branch after it.
+__device__ __forceinline__ bool named_sync_producers_or(bool x) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"(uint32_t(x)), "n"(kTcProducers)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ void fold_scalar(float* hi, float* lo, float x) {
+  float a = *hi;
+  float sum = a + x;
+  float bp = sum - a;
+  float err = (a - (sum - bp)) + (x - bp);
+  *hi = sum;
+  *lo += err;
+}
+
+// Drain TMEM into the float-float pair accumulators (producer threads).
+__device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, float* sVlof) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int q = warp & 3, h = warp >> 2;
+  const int r = 32 * q + lane, a = r >> 1, i = r & 1;
+  const bool row_ok = a < A.na;
+  const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(h * 128);
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1) named_sync_producers();
+    if (pass == 1 && h == 0) continue;
+    for (int c0 = 0; c0 < 128; c0 += 32) {
+      float v[32];
+      tc::tmem_ld32(lane_addr + c0, v);
+      if (!row_ok) continue;
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const int n = c0 + c, b = n >> 1, j = n & 1;
+        if (b >= A.na) continue;
+        if (pass == 0 && b >= a) {
+          const int e = pair_index(a, b, A.na) * 8 + (2 * i + j) * 2 + h;  // h=0: re, h=1: im
+          fold_scalar(sVf + e, sVlof + e, v[c]);
+        } else if (pass == 1 && b <= a) {
+          const int e = pair_index(b, a, A.na) * 8 + (2 * j + i) * 2 + 1;
+          fold_scalar(sVf + e, sVlof + e, -v[c]);
+        }
+      }
+    }
+  }
+  named_sync_producers();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float> A, SmemPlan S, TcPlan P) {
+  using L = StageLayout<MODE>;
+  constexpr int KAPPA = L::kKT / 4;  // sources per stage
+  extern __shared__ __align__(16) unsigned char smem[];
+  AntInfo<float>* sa = reinterpret_cast<AntInfo<float>*>(smem + S.off_ant);
+  SrcInfo<float>* ss = reinterpret_cast<SrcInfo<float>*>(smem + S.off_src);
+  Jones<float>* sV = reinterpret_cast<Jones<float>*>(smem + S.off_V);
+  Jones<float>* sVlo = reinterpret_cast<Jones<float>*>(smem + S.off_Vlo);
+  int* items = reinterpret_cast<int*>(smem + S.off_items);
+  double* red = reinterpret_cast<double*>(smem + S.off_red);
+  unsigned char* stage = smem + P.off_stage;
+  Jones<float>* sJ = reinterpret_cast<Jones<float>*>(stage);  // extended sources, after the tensor-core phase
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + P.off_bar);
+  uint64_t* full = bars;                    // [kTcStages], producers -> MMA
+  uint64_t* empty = bars + kTcStages;       // [kTcStages], MMA commit -> producers
+  uint64_t* accfull = bars + 2 * kTcStages;  // MMA commit -> producers (drain)
+  uint64_t* accfree = accfull + 1;           // producers -> MMA
+  uint64_t* done = accfull + 2;              // last MMA commit
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int unit = blockIdx.x;
+  const int t = unit / A.nchan, ch = unit - t * A.nchan;
+  if (tid == 0) *abort_flag = A.err ? *reinterpret_cast<volatile int*>(A.err) : 0;
+  __syncthreads();
+  if (*abort_flag) {  // an earlier CTA timed out: do no work
+    if (tid == 0) A.partial[unit] = double(NAN);
+    return;
+  }
+  __syncthreads();
+  load_antennas(A, t, ch, sa);
+  for (int i = tid; i < S.npairs; i += blockDim.x) {
+    sV[i] = jzero<float>();
+    sVlo[i] = jzero<float>();
+  }
+  if (tid == 0) {
+    const int npt = (A.na + 1) / 2, nqt = (A.na + 3) / 4;
+    int k = 0;
+    for (int ip = 0; ip < npt; ++ip)
+      for (int jq = (ip * 2) / 4; jq < nqt; ++jq) items[k++] = ip | (jq << 16);
+    for (int i = 0; i < kTcStages; ++i) {
+      tc::mbar_init(full + i, kTcProducers);
+      tc::mbar_init(empty + i, 1);
+    }
+    tc::mbar_init(accfull, 1);
+    tc::mbar_init(accfree, kTcProducers);
+    tc::mbar_init(done, 1);
+  }
+  if (warp == 8) tc::tmem_alloc(tmem_slot, kTcCols);
+  tc::fence_before_thread_sync();
+  __syncthreads();
+  tc::fence_after_thread_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  const float f = A.freq[ch];
+  const double nu_over_c = double(f) / kLightSpeed;
+  const ChanPos<float> cp = chan_pos<float>(f, A.lfreq, A.ufreq, A.nud);
+  const int nstages = (A.npsrc + KAPPA - 1) / KAPPA;
+  const int group = P.group;
+
+  if (warp < 8) {
+    // ---- producers -------------------------------------------------------
+    // Every break below follows an OR-vote over all producers, so they leave
+    // the loop together; the MMA warp never blocks them on a barrier.
+    bool bad = false;
+    for (int g = 0; g < nstages; ++g) {
+      const int slot = g % kTcStages, use = g / kTcStages;
+      bad = !tc::mbar_wait(empty + slot, (use & 1) ^ 1);
+      if (named_sync_producers_or(bad)) { bad = true; break; }
+      const int s0 = g * KAPPA, ns = min(KAPPA, A.npsrc - s0);
+      load_sources(A, t, ch, s0, ns, ss);
+      named_sync_producers();
+      unsigned char* hi = stage + size_t(slot) * 2 * L::kMatBytes;
+      unsigned char* lo = hi + L::kMatBytes;
+      for (int it = tid; it < KAPPA * 64; it += kTcProducers) {
+        const int sl = it >> 6, a = it & 63;
+        Jones<float> J = (a < A.na && sl < ns) ? compute_jones(A, t, s0 + sl, a, ss[sl], sa[a], f, nu_over_c, cp)
+                                               : jzero<float>();
+        L::put2(hi, lo, 2 * a, 2 * sl, J.a.r, J.b.r);
+        L::put2(hi, lo, 2 * a, 2 * KAPPA + 2 * sl, J.a.i, J.b.i);
+        L::put2(hi, lo, 2 * a + 1, 2 * sl, J.c.r, J.d.r);
+        L::put2(hi, lo, 2 * a + 1, 2 * KAPPA + 2 * sl, J.c.i, J.d.i);
+      }
+      tc::fence_proxy_async_smem();
+      tc::mbar_arrive(full + slot);
+      if ((g % group) == group - 1 || g == nstages - 1) {
+        bad = !tc::mbar_wait(accfull, (g / group) & 1);
+        tc::fence_after_thread_sync();
+        if (named_sync_producers_or(bad)) { bad = true; break; }
+        tc_drain(A, tmem, reinterpret_cast<float*>(sV), reinterpret_cast<float*>(sVlo));
+        tc::fence_before_thread_sync();
+        tc::mbar_arrive(accfree);
+      }
+    }
+    if (bad && tid == 0) *abort_flag = 1;
+  } else if (lane == 0) {
+    // ---- MMA issue ---------------------------------------------------------
+    const uint32_t idesc = L::instr(128, 128);
+    const int half = L::kKSteps / 2;
+    bool issued = false;
+    for (int g = 0; g < nstages && !*abort_flag; ++g) {
+      const int slot = g % kTcStages, use = g / kTcStages;
+      const bool first = (g % group) == 0;
+      if (first && g > 0) {
+        if (!tc::mbar_wait(accfree, ((g / group) - 1) & 1)) { *abort_flag = 1; break; }
+        tc::fence_after_thread_sync();
+      }
+      if (!tc::mbar_wait(full + slot, use & 1)) { *abort_flag = 1; break; }
+      tc::fence_after_thread_sync();
+      const uint32_t hi = tc::smem_addr(stage + size_t(slot) * 2 * L::kMatBytes);
+      const uint32_t lo = hi + L::kMatBytes;
+#pragma unroll
+      for (int kk = 0; kk < L::kKSteps; ++kk) {
+        const uint32_t o = kk * L::kKStepBytes;
+        const uint64_t ah = L::desc(hi + o), al = L::desc(lo + o);
+        L::mma(tmem, ah, ah, idesc, (first && kk == 0) ? 0u : 1u);
+        L::mma(tmem, ah, al, idesc, 1u);
+        L::mma(tmem, al, ah, idesc, 1u);
+      }
+#pragma unroll
+      for (int kk = 0; kk < half; ++kk) {
+        const uint32_t oi = (kk + half) * L::kKStepBytes, orr = kk * L::kKStepBytes;
+        const uint64_t ih = L::desc(hi + oi), il = L::desc(lo + oi);
+        const uint64_t rh = L::desc(hi + orr), rl = L::desc(lo + orr);
+        L::mma(tmem + 128, ih, rh, idesc, (first && kk == 0) ? 0u : 1u);
+        L::mma(tmem + 128, ih, rl, idesc, 1u);
+        L::mma(tmem + 128, il, rh, idesc, 1u);
+      }
+      issued = true;
+      tc::mma_commit(empty + slot);
+      if ((g % group) == group - 1 || g == nstages - 1) tc::mma_commit(accfull);
+    }
+    if (issued) {  // all MMAs finished before TMEM is released
+      tc::mma_commit(done);
+      if (!tc::mbar_wait(done, 0)) *abort_flag = 1;
+    }
+  }
+  tc::fence_before_thread_sync();
+  __syncthreads();
+  tc::fence_after_thread_sync();
+  if (warp == 8) tc::tmem_dealloc(tmem, kTcCols);
+  const bool aborted = *abort_flag != 0;
+
+  // ---- extended sources on the CUDA cores --------------------------------
+  const float kg = A.gauss_scale * f, ks = A.two_pi_over_c * f;
+  for (int s0 = A.npsrc; s0 < A.nsrc && !aborted;) {
+    const int s1 = min(s0 + S.st, A.nsrc), ns = s1 - s0;
+    load_sources(A, t, ch, s0, ns, ss);
+    __syncthreads();
+    produce_jones(A, S, t, ch, s0, ns, ss, sa, sJ, cp);
+    __syncthreads();
+    consume_pairs<float, 2, 4>(A, S, ns, ss, sa, sJ, sV, sVlo, items, true, kg, ks);
+    __syncthreads();
+    s0 = s1;
+  }
+  for (int i = tid; i < S.npairs; i += blockDim.x) sV[i] = jadd(sV[i], sVlo[i]);
+  __syncthreads();
+  epilogue(A, t, ch, unit, sV, sJ, red);
+  __syncthreads();
+  if (aborted && tid == 0) {
+    A.partial[unit] = double(NAN);
+    if (A.err) atomicExch(A.err, int(MB_ERR_TIMEOUT));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -530,7 +828,7 @@ __device__ void adj_consume_ext(const FusedArgs<T>& A, const SmemPlan& S, int ns
 // Chain d chi^2 / dJ through E, K and sqrt(B) to the source parameters.
 template <typename T>
 __device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int ch, int s0, int ns,
-                          const SrcInfo<T>* ss, const AntInfo<T>* sa, const double* sad, const Jones<T>* sgJ,
+                          const SrcInfo<T>* ss, const AntInfo<T>* sa, const Jones<T>* sgJ,
                           T* sacc, const ChanPos<T>& cp) {
   const T f = A.freq[ch];
   const double nu_over_c = double(f) / kLightSpeed;
@@ -561,11 +859,8 @@ __device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int c
     Jones<T> gKB = jhmul(E, gJ);
     Cx<T> gK = cmulc(gKB.a, B.a) + cmulc(gKB.b, B.b) + cmulc(gKB.c, B.c) + cmulc(gKB.d, B.d);
     T gphi = T(dphase) * (gK.r * K.i - gK.i * K.r);
-    double lD = double(src.l), mD = double(src.m);
-    double nfull = sqrt(1.0 - lD * lD - mD * mD);
-    double u = sad[3 * a], v = sad[3 * a + 1], w = sad[3 * a + 2];
-    gl0 += T(double(gphi) * (u - w * lD / nfull));
-    gm0 += T(double(gphi) * (v - w * mD / nfull));
+    gl0 += gphi * (ai.u - ai.w * src.l_over_n);
+    gm0 += gphi * (ai.v - ai.w * src.m_over_n);
     Cx<T> Kc = conj(K);
     Jones<T> gB = {cmul(Kc, gKB.a), cmul(Kc, gKB.b), cmul(Kc, gKB.c), cmul(Kc, gKB.d)};
     T GB = jdot_re(gB, B);
@@ -612,7 +907,6 @@ template <typename T, int RA, int RS>
 __global__ void __launch_bounds__(kFusedThreads) coh_adj_kernel(FusedArgs<T> A, SmemPlan S) {
   extern __shared__ __align__(16) unsigned char smem[];
   AntInfo<T>* sa = reinterpret_cast<AntInfo<T>*>(smem + S.off_ant);
-  double* sad = reinterpret_cast<double*>(smem + S.off_antd);
   SrcInfo<T>* ss = reinterpret_cast<SrcInfo<T>*>(smem + S.off_src);
   Jones<T>* sJ = reinterpret_cast<Jones<T>*>(smem + S.off_J);
   Jones<T>* sgJ = reinterpret_cast<Jones<T>*>(smem + S.off_gJ);
@@ -621,7 +915,7 @@ __global__ void __launch_bounds__(kFusedThreads) coh_adj_kernel(FusedArgs<T> A, 
 
   const int unit = blockIdx.x;
   const int t = unit / A.nchan, ch = unit - t * A.nchan;
-  load_antennas(A, t, ch, sa, sad);
+  load_antennas(A, t, ch, sa);
   for (int i = threadIdx.x; i < S.npairs; i += blockDim.x) sX[i] = jzero<T>();
   for (int i = threadIdx.x; i < S.st * kNAcc; i += blockDim.x) sacc[i] = T(0);
   __syncthreads();
@@ -648,7 +942,7 @@ __global__ void __launch_bounds__(kFusedThreads) coh_adj_kernel(FusedArgs<T> A, 
     if (s0 < A.npsrc) adj_consume_point<T, RA, RS>(A, S, ns, sJ, sX, sgJ);
     else adj_consume_ext<T>(A, S, ns, ss, sa, sJ, sX, sgJ, sacc, kg, ks);
     __syncthreads();
-    adj_chain<T>(A, S, t, ch, s0, ns, ss, sa, sad, sgJ, sacc, cp);
+    adj_chain<T>(A, S, t, ch, s0, ns, ss, sa, sgJ, sacc, cp);
     __syncthreads();
     adj_flush<T>(A, t, s0, ns, sacc);
     __syncthreads();
@@ -711,7 +1005,7 @@ __global__ void finalize_grads_kernel(FusedArgs<T> A, double scale, T* __restric
 // Host side
 // ---------------------------------------------------------------------------
 struct WsLayout {
-  size_t phi, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, tc, total;
+  size_t phi, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, err, total;
 };
 
 WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_grad) {
@@ -731,7 +1025,7 @@ WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_gra
   L.acc_gauss = take(want_grad ? 3 * ng * 8 : 0);
   L.acc_sersic = take(want_grad ? 3 * nx * 8 : 0);
   L.acc_end = o;
-  L.tc = take(mode != MB_MODE_NATIVE ? tc_scratch_bytes(d) : 0);
+  L.err = take(sizeof(int));
   L.total = o;
   return L;
 }
@@ -764,7 +1058,7 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.sersic = (const T*)in->sersic_shape; A.weight = (const T*)in->weight_vector; A.obs = (const T*)in->observed_vis;
   A.ant1 = in->antenna1; A.ant2 = in->antenna2; A.flag = in->flag;
   A.model_vis = (T*)model_vis; A.chi2 = (T*)chi2;
-  A.Vpoint = nullptr;
+  A.err = nullptr;
   A.phi = nullptr; A.partial = nullptr; A.gV = nullptr; A.dG = nullptr;
   A.acc_lm = A.acc_stokes = A.acc_alpha = A.acc_gauss = A.acc_sersic = nullptr;
   if (ws == nullptr) return MB_OK;
@@ -778,6 +1072,7 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.acc_alpha = reinterpret_cast<double*>(w + L.acc_alpha);
   A.acc_gauss = reinterpret_cast<double*>(w + L.acc_gauss);
   A.acc_sersic = reinterpret_cast<double*>(w + L.acc_sersic);
+  A.err = reinterpret_cast<int*>(w + L.err);
   return MB_OK;
 }
 
@@ -808,6 +1103,47 @@ mb_status check_inputs(const mb_dims* d, const mb_props* P, uint32_t options, co
   return MB_OK;
 }
 
+mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2, cudaStream_t stream) {
+  if (A.na > 64)
+    return fail(MB_ERR_UNSUPPORTED, "split-precision modes handle up to 64 antennas (got %d)", A.na);
+  const int units = A.ntime * A.nchan;
+  SmemPlan S = make_plan<float>(A.na, false);
+  // The tensor-core kernel runs with kTcThreads threads; its extended-source
+  // phase uses the same pair-tile plan with that thread count.
+  S.nthreads = kTcThreads;
+  S.groups = S.nitems <= kTcThreads ? std::min(8, std::max(1, kTcThreads / S.nitems)) : 1;
+  TcPlan P;
+  P.group = kTcGroup;
+  if (const char* g = getenv("MB_TC_GROUP")) P.group = std::max(1, atoi(g));
+  // Stage buffers first (128-byte aligned), then the CUDA-core plan's regions,
+  // shifted; the extended-source Jones tile reuses the stage buffers.
+  const size_t stage_bytes = size_t(kTcStages) * 2 * StageGeometry::kMatBytes;
+  const size_t need_J = sizeof(Jones<float>) * S.st * S.nap;
+  const size_t stage_region = align_up(std::max(stage_bytes, need_J), 128);
+  P.off_stage = 0;
+  S.off_ant += stage_region; S.off_src += stage_region; S.off_V += stage_region;
+  S.off_Vlo += stage_region; S.off_items += stage_region; S.off_red += stage_region;
+  S.off_J = 0;
+  P.off_bar = align_up(S.total + stage_region, 16);
+  P.total = P.off_bar + (2 * kTcStages + 3) * sizeof(uint64_t) + 16;
+  if (P.total > 227 * 1024)
+    return fail(MB_ERR_UNSUPPORTED, "split-precision kernel needs %zu bytes of shared memory for na=%d",
+                P.total, A.na);
+  if (A.err) MB_CUDA(cudaMemsetAsync(A.err, 0, sizeof(int), stream));
+  if (mode == MB_MODE_SPLIT_TF32) {
+    auto kern = coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32>;
+    MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
+    kern<<<units, kTcThreads, P.total, stream>>>(A, S, P);
+  } else {
+    auto kern = coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16>;
+    MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
+    kern<<<units, kTcThreads, P.total, stream>>>(A, S, P);
+  }
+  MB_CHECK(check_launch("coh_tc_fwd_kernel"));
+  sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, A.weights ? 1.0 : A.inv_sigma2, X2);
+  return check_launch("sum_partials_kernel");
+}
+
 template <typename T>
 mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* ws, const WsLayout& L,
                          cudaStream_t stream) {
@@ -824,14 +1160,10 @@ mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* 
       MB_CHECK(check_launch("phi_kernel"));
     }
   }
-  FusedArgs<T> B = A;
   if constexpr (sizeof(T) == 4) {
-    if (mode != MB_MODE_NATIVE && A.npsrc > 0) {
-      float* Vp = reinterpret_cast<float*>(static_cast<char*>(ws) + L.tc);
-      MB_CHECK(tc_point_coherencies(A, mode, Vp, stream));
-      B.Vpoint = Vp;
-    }
+    if (mode != MB_MODE_NATIVE) return launch_tc_forward(A, mode, X2, stream);
   }
+  const FusedArgs<T>& B = A;
   constexpr int RP = FwdTile<T>::RP, RQ = FwdTile<T>::RQ;
   SmemPlan S = make_plan<T>(A.na, false);
   if (S.total > 227 * 1024)
@@ -839,7 +1171,7 @@ mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* 
                 S.total, A.na);
   auto kern = coh_fwd_kernel<T, RP, RQ>;
   MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
-  kern<<<units, kFusedThreads, S.total, stream>>>(B, S);
+  kern<<<units, S.nthreads, S.total, stream>>>(B, S);
   MB_CHECK(check_launch("coh_fwd_kernel"));
   const double scale = A.weights ? 1.0 : A.inv_sigma2;
   sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, scale, X2);
@@ -859,7 +1191,7 @@ mb_status launch_adjoint(const FusedArgs<T>& A, double grad_scale, const mb_rime
       return fail(MB_ERR_UNSUPPORTED, "fused adjoint needs %zu bytes of shared memory for na=%d", S.total, A.na);
     auto kern = coh_adj_kernel<T, RA, RS>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
-    kern<<<units, kFusedThreads, S.total, stream>>>(A, S);
+    kern<<<units, S.nthreads, S.total, stream>>>(A, S);
     MB_CHECK(check_launch("coh_adj_kernel"));
   }
   size_t total = size_t(A.nsrc) * 2 + size_t(A.nsrc) * A.ntime + 3 * size_t(A.ngsrc) + 3 * size_t(A.nssrc) +
@@ -932,7 +1264,7 @@ mb_status launch_forward_noalloc(FusedArgs<T> A, double* partials, double* X2, c
                 S.total, A.na);
   auto kern = coh_fwd_kernel<T, RP, RQ>;
   MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
-  kern<<<units, kFusedThreads, S.total, stream>>>(A, S);
+  kern<<<units, S.nthreads, S.total, stream>>>(A, S);
   MB_CHECK(check_launch("coh_fwd_kernel"));
   sum_partials_kernel<<<1, 1024, 0, stream>>>(partials, units, A.weights ? 1.0 : A.inv_sigma2, X2);
   return check_launch("sum_partials_kernel");

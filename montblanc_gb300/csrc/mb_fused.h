@@ -33,14 +33,13 @@ struct FusedArgs {
   T* dG;              // (ntime, na, nchan, 4) complex d chi^2 / d G
   // adjoint accumulators (FP64)
   double *acc_lm, *acc_stokes, *acc_alpha, *acc_gauss, *acc_sersic;
-  // the point-source coherencies come from the tensor-core kernel
-  const float* Vpoint;  // (ntime*nchan, na*na) packed by mb_tc.cu, or NULL
+  int* err;  // device error word (bounded waits that gave up), or NULL
 };
 
 // Per-antenna data for one (time, channel) unit.
 template <typename T>
 struct AntInfo {
-  T sin_pa, cos_pa, pe_l, pe_m, sc_l, sc_m, u, v;
+  T sin_pa, cos_pa, pe_l, pe_m, sc_l, sc_m, u, v, w;
 };
 
 // Per-source data for one (time, channel) unit.
@@ -50,6 +49,7 @@ struct SrcInfo {
   T l, m;            // direction cosines
   T s0, s1, s2;      // shape parameters (gaussian el, em, R / sersic e1, e2, R)
   T power, I, Q, U, V;
+  T l_over_n, m_over_n;  // l / sqrt(1 - l^2 - m^2), m / sqrt(1 - l^2 - m^2)
   int type;
   int pad;
 };
@@ -60,10 +60,13 @@ struct SmemPlan {
   int st;           // sources per tile
   int npairs;       // na (na + 1) / 2
   int nitems;       // pair tiles
-  size_t off_ant, off_antd, off_src, off_J, off_gJ, off_V, off_items, off_acc, off_red, total;
+  int nthreads;     // threads per CTA
+  int groups;       // source groups sharing each pair tile (forward)
+  size_t off_ant, off_antd, off_src, off_J, off_gJ, off_V, off_Vlo, off_items, off_acc, off_red, total;
 };
 
 constexpr int kFusedThreads = 256;
+constexpr int kFwdMaxThreads = 320;
 
 size_t fused_workspace_size(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_grad);
 

@@ -1,17 +1,110 @@
-// Tensor-core (tcgen05) point-source coherencies: placeholder until the
-// split-precision GEMM lands.
+// Tensor-core diagnostics: a one-CTA split-precision GEMM that exercises
+// exactly the operand staging (no-swizzle K-major core-matrix layout),
+// descriptors, tcgen05.mma, commit and TMEM readout used by the fused
+// split-precision coherency kernel in mb_fused.cu.
 #include "mb_fused.h"
+#include "mb_tc_layout.cuh"
+#include "mb_tcgen05.cuh"
 
 namespace mb {
 
-size_t tc_scratch_bytes(const mb_dims* d) {
-  const size_t na = ext(d->na);
-  return size_t(ext(d->ntime)) * ext(d->nchan) * na * na * 8 * sizeof(float);
+namespace {
+
+// D (128 x 128) = A (128 x K) . B (128 x K)^T, both row-major FP32, K a
+// multiple of 32; split into hi + lo parts, 3 products, FP32 accumulation.
+// Threads 0..127 stage operands and read TMEM; warp 4 issues the MMAs.
+template <int MODE>
+__global__ void __launch_bounds__(160) tc_selftest_kernel(const float* __restrict__ A, const float* __restrict__ B,
+                                                          int K, float* __restrict__ D, int* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  using L = StageLayout<MODE>;
+  unsigned char* sA_hi = smem;
+  unsigned char* sA_lo = smem + L::kMatBytes;
+  unsigned char* sB_hi = smem + 2 * L::kMatBytes;
+  unsigned char* sB_lo = smem + 3 * L::kMatBytes;
+  __shared__ uint64_t bar_mma;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar_mma, 1);
+    abort_flag = 0;
+  }
+  if (warp == 4) tc::tmem_alloc(&tmem_base, 128);
+  tc::fence_before_thread_sync();
+  __syncthreads();
+  tc::fence_after_thread_sync();
+  const uint32_t tmem = tmem_base;
+  const uint32_t idesc = L::instr(128, 128);
+  int phase = 0;
+  for (int k0 = 0; k0 < K; k0 += L::kKT) {
+    if (threadIdx.x < 128) {
+      const int r = threadIdx.x;
+      for (int k = 0; k < L::kKT; ++k) {
+        L::put(sA_hi, sA_lo, r, k, A[size_t(r) * K + k0 + k]);
+        L::put(sB_hi, sB_lo, r, k, B[size_t(r) * K + k0 + k]);
+      }
+      tc::fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (warp == 4 && lane == 0) {
+      tc::fence_after_thread_sync();
+      for (int kk = 0; kk < L::kKSteps; ++kk) {
+        const uint32_t off = kk * L::kKStepBytes;
+        uint64_t ah = L::desc(tc::smem_addr(sA_hi) + off), al = L::desc(tc::smem_addr(sA_lo) + off);
+        uint64_t bh = L::desc(tc::smem_addr(sB_hi) + off), bl = L::desc(tc::smem_addr(sB_lo) + off);
+        L::mma(tmem, ah, bh, idesc, (k0 > 0 || kk > 0) ? 1u : 0u);
+        L::mma(tmem, ah, bl, idesc, 1u);
+        L::mma(tmem, al, bh, idesc, 1u);
+      }
+      tc::mma_commit(&bar_mma);
+      if (!tc::mbar_wait(&bar_mma, phase)) atomicExch(&abort_flag, 1);
+    }
+    phase ^= 1;
+    __syncthreads();  // operands may be overwritten only after the MMAs finished
+  }
+  tc::fence_after_thread_sync();
+  if (warp < 4) {
+    const int r = warp * 32 + lane;
+    for (int c0 = 0; c0 < 128; c0 += 32) {
+      float v[32];
+      tc::tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + c0, v);
+      for (int i = 0; i < 32; ++i) D[size_t(r) * 128 + c0 + i] = v[i];
+    }
+  }
+  tc::fence_before_thread_sync();
+  __syncthreads();
+  if (warp == 4) tc::tmem_dealloc(tmem, 128);
+  if (threadIdx.x == 0 && abort_flag) *status = 1;
 }
 
-mb_status tc_point_coherencies(const FusedArgs<float>& A, mb_mode mode, float* Vpoint, cudaStream_t stream) {
-  (void)A; (void)mode; (void)Vpoint; (void)stream;
-  return fail(MB_ERR_UNSUPPORTED, "split-precision tensor-core path not built");
-}
+}  // namespace
 
 }  // namespace mb
+
+using namespace mb;
+
+extern "C" {
+
+mb_status mb_tc_selftest(const float* A, const float* B, int K, int mode, float* D, int* status, void* stream) {
+  MB_REQUIRE(A, "A"); MB_REQUIRE(B, "B"); MB_REQUIRE(D, "D"); MB_REQUIRE(status, "status");
+  const int kt = mode == MB_MODE_SPLIT_BF16 ? 64 : 32;
+  if (K <= 0 || K % kt != 0) return fail(MB_ERR_INVALID_ARG, "K must be a positive multiple of %d (got %d)", kt, K);
+  cudaStream_t s = as_stream(stream);
+  if (mode == MB_MODE_SPLIT_TF32) {
+    const size_t smem = 4 * StageLayout<MB_MODE_SPLIT_TF32>::kMatBytes;
+    MB_CUDA(cudaFuncSetAttribute(tc_selftest_kernel<MB_MODE_SPLIT_TF32>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    tc_selftest_kernel<MB_MODE_SPLIT_TF32><<<1, 160, smem, s>>>(A, B, K, D, status);
+  } else if (mode == MB_MODE_SPLIT_BF16) {
+    const size_t smem = 4 * StageLayout<MB_MODE_SPLIT_BF16>::kMatBytes;
+    MB_CUDA(cudaFuncSetAttribute(tc_selftest_kernel<MB_MODE_SPLIT_BF16>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    tc_selftest_kernel<MB_MODE_SPLIT_BF16><<<1, 160, smem, s>>>(A, B, K, D, status);
+  } else {
+    return fail(MB_ERR_INVALID_ARG, "mode must be a split-precision mode");
+  }
+  return check_launch("tc_selftest_kernel");
+}
+
+}  // extern "C"
