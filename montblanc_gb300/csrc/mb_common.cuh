@@ -334,6 +334,44 @@ __device__ __forceinline__ Jones<T> beam_interp(const T* __restrict__ E_beam, co
   return E;
 }
 
+// The beam cube blended along frequency for one channel: per (l, m) grid
+// cell the 4 correlations of E (complex) and of |E|, each linearly
+// interpolated between the two channel planes the channel falls between.
+// Trilinear interpolation of the cube is then a bilinear interpolation of
+// this plane with the same weights (sum over 8 corners = sum over 4 corners
+// of the channel-blended values).  Layout: [il][im][12] = E (4 complex),
+// |E| (4 real).
+constexpr int kPlaneVals = 12;
+
+template <typename T>
+__device__ __forceinline__ void plane_corner(const T* __restrict__ plane, int mh, int il, int im, T w,
+                                             Jones<T>& sum, T (&amp)[4]) {
+  const T* p = plane + kPlaneVals * (size_t(il) * mh + im);
+  Jones<T> e = jldg<T>(p);
+  sum.a = sum.a + e.a * w; sum.b = sum.b + e.b * w;
+  sum.c = sum.c + e.c * w; sum.d = sum.d + e.d * w;
+  amp[0] += w * __ldg(p + 8); amp[1] += w * __ldg(p + 9);
+  amp[2] += w * __ldg(p + 10); amp[3] += w * __ldg(p + 11);
+}
+
+template <typename T>
+__device__ __forceinline__ Jones<T> beam_interp_plane(const T* __restrict__ plane, int mh, const GridPos<T>& gl,
+                                                      const GridPos<T>& gm) {
+  Jones<T> sum = jzero<T>();
+  T amp[4] = {T(0), T(0), T(0), T(0)};
+  const T ld = gl.d, md = gm.d;
+  plane_corner(plane, mh, gl.i0, gm.i0, (T(1) - ld) * (T(1) - md), sum, amp);
+  plane_corner(plane, mh, gl.i1, gm.i0, ld * (T(1) - md), sum, amp);
+  plane_corner(plane, mh, gl.i0, gm.i1, (T(1) - ld) * md, sum, amp);
+  plane_corner(plane, mh, gl.i1, gm.i1, ld * md, sum, amp);
+  Jones<T> E;
+  E.a = renorm(sum.a, amp[0]);
+  E.b = renorm(sum.b, amp[1]);
+  E.c = renorm(sum.c, amp[2]);
+  E.d = renorm(sum.d, amp[3]);
+  return E;
+}
+
 // Rotate (l, m) by the parallactic angle, add the pointing error and scale
 // by the antenna scaling (CPUSolver.py:367-390).
 template <typename T>

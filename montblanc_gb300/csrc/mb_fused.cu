@@ -38,10 +38,11 @@ template <typename T> struct FwdTile;
 template <> struct FwdTile<float> { static constexpr int RP = 2, RQ = 4, ST = 16; };
 template <> struct FwdTile<double> { static constexpr int RP = 1, RQ = 2, ST = 8; };
 template <typename T> struct AdjTile;
-template <> struct AdjTile<float> { static constexpr int RA = 2, RS = 4, ST = 32; };
-template <> struct AdjTile<double> { static constexpr int RA = 1, RS = 2, ST = 8; };
+template <> struct AdjTile<float> { static constexpr int RA = 2, RS = 2, ST = 32, THREADS = 512; };
+template <> struct AdjTile<double> { static constexpr int RA = 1, RS = 2, ST = 8, THREADS = 256; };
 
 constexpr int kNAcc = 10;  // l, m, I, Q, U, V, alpha, shape0, shape1, shape2
+constexpr int kBsqVals = 8;  // values per (source, time) entry of the sqrt(B) table
 
 int count_pair_tiles(int na, int RP, int RQ) {
   int npt = (na + RP - 1) / RP, nqt = (na + RQ - 1) / RQ, n = 0;
@@ -57,7 +58,7 @@ SmemPlan make_plan(int na, bool adjoint) {
   S.npairs = na * (na + 1) / 2;
   S.nitems = count_pair_tiles(na, FwdTile<T>::RP, FwdTile<T>::RQ);
   if (adjoint) {
-    S.nthreads = kFusedThreads;
+    S.nthreads = AdjTile<T>::THREADS;
     S.groups = 1;
   } else if (S.nitems <= kFwdMaxThreads) {
     // one pair tile per thread; spare threads split each tile's sources
@@ -161,14 +162,15 @@ __device__ __forceinline__ Cx<T> phase_term(const FusedArgs<T>& A, int t, int s,
 template <typename T>
 __device__ __forceinline__ Jones<T> compute_jones(const FusedArgs<T>& A, int t, int s, int a, const SrcInfo<T>& src,
                                                   const AntInfo<T>& ai, T f, double nu_over_c,
-                                                  const ChanPos<T>& cp) {
+                                                  const ChanPos<T>& cp, int plane_ch) {
   const BeamGeom G{A.lw, A.mh, A.nud};
   Cx<T> K = phase_term(A, t, s, a, f, nu_over_c);
   T l, m;
   beam_lm<T>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
   GridPos<T> gl = grid_pos<T>(l, A.ll, A.ul, A.lscale, A.lw);
   GridPos<T> gm = grid_pos<T>(m, A.lmm, A.um, A.mscale, A.mh);
-  Jones<T> E = beam_interp<T>(A.E_beam, G, gl, gm, cp);
+  Jones<T> E = A.plane ? beam_interp_plane<T>(A.plane + size_t(plane_ch) * A.lw * A.mh * kPlaneVals, A.mh, gl, gm)
+                       : beam_interp<T>(A.E_beam, G, gl, gm, cp);
   Jones<T> KB = {cmul(K, src.B.a), cmul(K, src.B.b), cmul(K, src.B.c), cmul(K, src.B.d)};
   return jmul(E, KB);
 }
@@ -181,7 +183,7 @@ __device__ void produce_jones(const FusedArgs<T>& A, const SmemPlan& S, int t, i
   const double nu_over_c = double(f) / kLightSpeed;
   for (int i = threadIdx.x; i < ns * S.nap; i += blockDim.x) {
     int si = i / S.nap, a = i - si * S.nap;
-    sJ[i] = a < A.na ? compute_jones(A, t, s0 + si, a, ss[si], sa[a], f, nu_over_c, cp) : jzero<T>();
+    sJ[i] = a < A.na ? compute_jones(A, t, s0 + si, a, ss[si], sa[a], f, nu_over_c, cp, ch) : jzero<T>();
   }
 }
 
@@ -436,15 +438,21 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A,
 // Re J_s,a[i][c] (K index 2s + c) and Im J_s,a[i][c] (K index 2k + 2s + c):
 //   D_re = A A^T            = Re sum_s J_a J_b^H  (rows 2a+i, columns 2b+j)
 //   D_x  = A_im A_re^T,  Im sum_s J_a J_b^H = D_x - D_x^T,
-// with each operand value split into hi + lo parts and D += hi.hi + hi.lo +
-// lo.hi, FP32 accumulation in TMEM over kTcGroup stages, then folded into
-// float-float pair accumulators in shared memory (so the sum over all
-// sources keeps better than FP32 precision).
+// with each operand value split into hi + lo parts: the large hi.hi products
+// and the small hi.lo + lo.hi corrections accumulate in separate TMEM
+// accumulators (FP32), which are folded into float-float pair accumulators
+// in shared memory every kTcGroup stages.  The tensor core's FP32
+// accumulation rounds toward zero, so its error grows with the number of
+// accumulations into one accumulator (about 2.5e-8 of the result per
+// accumulation for a coherent sum); short groups keep the sum over all
+// sources near 1e-7 relative.
 constexpr int kTcProducers = 256;          // warps 0-7: operands, TMEM drain
 constexpr int kTcThreads = kTcProducers + 32;  // warp 8: MMA issue
-constexpr int kTcStages = 2;
+constexpr int kTcStages = 3;
+constexpr int kTcRowBytes = 64;  // 4 sources (TF32) / 8 sources (BF16) per stage
 constexpr int kTcGroup = 16;               // stages per TMEM accumulation group
-constexpr uint32_t kTcCols = 256;          // D_re: columns 0-127, D_x: 128-255
+// TMEM columns: D_re 0-127, D_x 128-255 (hi.hi); their corrections 256-511.
+constexpr uint32_t kTcCols = 512;
 
 struct TcPlan {
   size_t off_stage, off_bar, total;
@@ -488,8 +496,11 @@ __device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, f
     if (pass == 1) named_sync_producers();
     if (pass == 1 && h == 0) continue;
     for (int c0 = 0; c0 < 128; c0 += 32) {
-      float v[32];
+      float v[32], w[32];
       tc::tmem_ld32(lane_addr + c0, v);
+      tc::tmem_ld32(lane_addr + 256 + c0, w);
+#pragma unroll
+      for (int c = 0; c < 32; ++c) v[c] += w[c];
       if (!row_ok) continue;
 #pragma unroll
       for (int c = 0; c < 32; ++c) {
@@ -508,9 +519,32 @@ __device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, f
   named_sync_producers();
 }
 
+// Source terms needed for a point source's J at (time t, channel ch).
+__device__ __forceinline__ SrcInfo<float> point_source_info(const FusedArgs<float>& A, int t, int ch, int s,
+                                                           float log2_ratio) {
+  SrcInfo<float> si;
+  si.l = __ldg(A.lm + 2 * s);
+  si.m = __ldg(A.lm + 2 * s + 1);
+  if (A.bsq0) {  // sqrt(B) = (nu/nu_ref)^(alpha/2) sqrt(B)(nu_ref)
+    const float* b = A.bsq0 + kBsqVals * (size_t(s) * A.ntime + t);
+    const float4 q = __ldg(reinterpret_cast<const float4*>(b));
+    const float sp = exp2f(__ldg(b + 4) * log2_ratio);
+    si.B.a = {sp * q.x, 0.f};
+    si.B.b = {sp * q.z, sp * q.w};
+    si.B.c = {sp * q.z, -sp * q.w};
+    si.B.d = {sp * q.y, 0.f};
+    return si;
+  }
+  const size_t st = size_t(s) * A.ltime + t;
+  const float* S = A.stokes + 4 * st;
+  const float power = mb_pow(__ldg(A.freq + ch) / __ldg(A.ref_freq + ch), __ldg(A.alpha + st));
+  si.B = brightness_sqrt<float>(__ldg(S), __ldg(S + 1), __ldg(S + 2), __ldg(S + 3), power);
+  return si;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float> A, SmemPlan S, TcPlan P) {
-  using L = StageLayout<MODE>;
+  using L = StageLayout<MODE, kTcRowBytes>;
   constexpr int KAPPA = L::kKT / 4;  // sources per stage
   extern __shared__ __align__(16) unsigned char smem[];
   AntInfo<float>* sa = reinterpret_cast<AntInfo<float>*>(smem + S.off_ant);
@@ -569,34 +603,50 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   const ChanPos<float> cp = chan_pos<float>(f, A.lfreq, A.ufreq, A.nud);
   const int nstages = (A.npsrc + KAPPA - 1) / KAPPA;
   const int group = P.group;
+  const float log2_ratio = log2f(f / A.ref_freq[ch]);
 
   if (warp < 8) {
     // ---- producers -------------------------------------------------------
     // Every break below follows an OR-vote over all producers, so they leave
     // the loop together; the MMA warp never blocks them on a barrier.
+    // Item mapping: warp w covers antennas 8w .. 8w+7 and the stage's
+    // sources; lane bits 0-1 and 2 pick the antenna, bits 3-4 the source.
+    // Rows are written starting from row i0 = antenna bit 2, so that one
+    // store instruction of a warp touches all 8 rows of a core matrix and
+    // both halves of a 16-byte chunk (at most 2-way bank conflicts).
     bool bad = false;
+    const int a = 8 * warp + (lane & 3) + 4 * ((lane >> 2) & 1);
+    const int i0 = (lane >> 2) & 1;
+    // A producer whose wait gave up skips its work but keeps taking part in
+    // the group-end votes, where all producers leave the loop together.
     for (int g = 0; g < nstages; ++g) {
       const int slot = g % kTcStages, use = g / kTcStages;
-      bad = !tc::mbar_wait(empty + slot, (use & 1) ^ 1);
-      if (named_sync_producers_or(bad)) { bad = true; break; }
-      const int s0 = g * KAPPA, ns = min(KAPPA, A.npsrc - s0);
-      load_sources(A, t, ch, s0, ns, ss);
-      named_sync_producers();
-      unsigned char* hi = stage + size_t(slot) * 2 * L::kMatBytes;
-      unsigned char* lo = hi + L::kMatBytes;
-      for (int it = tid; it < KAPPA * 64; it += kTcProducers) {
-        const int sl = it >> 6, a = it & 63;
-        Jones<float> J = (a < A.na && sl < ns) ? compute_jones(A, t, s0 + sl, a, ss[sl], sa[a], f, nu_over_c, cp)
-                                               : jzero<float>();
-        L::put2(hi, lo, 2 * a, 2 * sl, J.a.r, J.b.r);
-        L::put2(hi, lo, 2 * a, 2 * KAPPA + 2 * sl, J.a.i, J.b.i);
-        L::put2(hi, lo, 2 * a + 1, 2 * sl, J.c.r, J.d.r);
-        L::put2(hi, lo, 2 * a + 1, 2 * KAPPA + 2 * sl, J.c.i, J.d.i);
+      if (!bad) bad = !tc::mbar_wait(empty + slot, (use & 1) ^ 1);
+      if (!bad) {
+        const int s0 = g * KAPPA, ns = min(KAPPA, A.npsrc - s0);
+        unsigned char* hi = stage + size_t(slot) * 2 * L::kMatBytes;
+        unsigned char* lo = hi + L::kMatBytes;
+#pragma unroll
+        for (int rep = 0; rep < KAPPA / 4; ++rep) {
+          const int sl = (lane >> 3) + 4 * rep;
+          Jones<float> J = jzero<float>();
+          if (a < A.na && sl < ns) {
+            const SrcInfo<float> src = point_source_info(A, t, ch, s0 + sl, log2_ratio);
+            J = compute_jones(A, t, s0 + sl, a, src, sa[a], f, nu_over_c, cp, ch);
+          }
+          // row 2a holds J00, J01; row 2a + 1 holds J10, J11
+          const Cx<float> r0a = i0 ? J.c : J.a, r0b = i0 ? J.d : J.b;
+          const Cx<float> r1a = i0 ? J.a : J.c, r1b = i0 ? J.b : J.d;
+          L::put2(hi, lo, 2 * a + i0, 2 * sl, r0a.r, r0b.r);
+          L::put2(hi, lo, 2 * a + i0, 2 * KAPPA + 2 * sl, r0a.i, r0b.i);
+          L::put2(hi, lo, 2 * a + 1 - i0, 2 * sl, r1a.r, r1b.r);
+          L::put2(hi, lo, 2 * a + 1 - i0, 2 * KAPPA + 2 * sl, r1a.i, r1b.i);
+        }
+        tc::fence_proxy_async_smem();
+        tc::mbar_arrive(full + slot);
       }
-      tc::fence_proxy_async_smem();
-      tc::mbar_arrive(full + slot);
       if ((g % group) == group - 1 || g == nstages - 1) {
-        bad = !tc::mbar_wait(accfull, (g / group) & 1);
+        if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1);
         tc::fence_after_thread_sync();
         if (named_sync_producers_or(bad)) { bad = true; break; }
         tc_drain(A, tmem, reinterpret_cast<float*>(sV), reinterpret_cast<float*>(sVlo));
@@ -621,22 +671,25 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
       tc::fence_after_thread_sync();
       const uint32_t hi = tc::smem_addr(stage + size_t(slot) * 2 * L::kMatBytes);
       const uint32_t lo = hi + L::kMatBytes;
+      const uint32_t acc0 = (first ? 0u : 1u);
 #pragma unroll
       for (int kk = 0; kk < L::kKSteps; ++kk) {
         const uint32_t o = kk * L::kKStepBytes;
         const uint64_t ah = L::desc(hi + o), al = L::desc(lo + o);
-        L::mma(tmem, ah, ah, idesc, (first && kk == 0) ? 0u : 1u);
-        L::mma(tmem, ah, al, idesc, 1u);
-        L::mma(tmem, al, ah, idesc, 1u);
+        const uint32_t acc = kk == 0 ? acc0 : 1u;
+        L::mma(tmem, ah, ah, idesc, acc);
+        L::mma(tmem + 256, ah, al, idesc, acc);
+        L::mma(tmem + 256, al, ah, idesc, 1u);
       }
 #pragma unroll
       for (int kk = 0; kk < half; ++kk) {
         const uint32_t oi = (kk + half) * L::kKStepBytes, orr = kk * L::kKStepBytes;
         const uint64_t ih = L::desc(hi + oi), il = L::desc(lo + oi);
         const uint64_t rh = L::desc(hi + orr), rl = L::desc(lo + orr);
-        L::mma(tmem + 128, ih, rh, idesc, (first && kk == 0) ? 0u : 1u);
-        L::mma(tmem + 128, ih, rl, idesc, 1u);
-        L::mma(tmem + 128, il, rh, idesc, 1u);
+        const uint32_t acc = kk == 0 ? acc0 : 1u;
+        L::mma(tmem + 128, ih, rh, idesc, acc);
+        L::mma(tmem + 384, ih, rl, idesc, acc);
+        L::mma(tmem + 384, il, rh, idesc, 1u);
       }
       issued = true;
       tc::mma_commit(empty + slot);
@@ -708,6 +761,50 @@ __device__ void beam_interp_d(const T* __restrict__ E_beam, const BeamGeom& G, c
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       T ab = cabs_(e4[k]);
+      s4[k] = s4[k] + e4[k] * w; amp[k] += w * ab;
+      l4[k] = l4[k] + e4[k] * wl; dal[k] += wl * ab;
+      m4[k] = m4[k] + e4[k] * wm; dam[k] += wm * ab;
+    }
+  }
+  Cx<T>* E4 = &E.a; Cx<T>* dl4 = &dEl.a; Cx<T>* dm4 = &dEm.a;
+  const Cx<T>* s4 = &sum.a; const Cx<T>* l4 = &dsl.a; const Cx<T>* m4 = &dsm.a;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    T r = cabs_(s4[k]);
+    T inv = T(1) / r;
+    if (isfinite(inv)) {
+      E4[k] = s4[k] * (amp[k] * inv);
+      T drl = cdot_re(s4[k], l4[k]) * inv, drm = cdot_re(s4[k], m4[k]) * inv;
+      dl4[k] = (l4[k] * amp[k] + s4[k] * dal[k]) * inv - s4[k] * (amp[k] * drl * inv * inv);
+      dm4[k] = (m4[k] * amp[k] + s4[k] * dam[k]) * inv - s4[k] * (amp[k] * drm * inv * inv);
+    } else {
+      E4[k] = s4[k] * amp[k];
+      dl4[k] = l4[k] * amp[k] + s4[k] * dal[k];
+      dm4[k] = m4[k] * amp[k] + s4[k] * dam[k];
+    }
+  }
+}
+
+// Same as beam_interp_d on the frequency-blended plane (4 corners).
+template <typename T>
+__device__ void beam_interp_plane_d(const T* __restrict__ plane, int mh, const GridPos<T>& gl, const GridPos<T>& gm,
+                                    Jones<T>& E, Jones<T>& dEl, Jones<T>& dEm) {
+  Jones<T> sum = jzero<T>(), dsl = jzero<T>(), dsm = jzero<T>();
+  T amp[4] = {0, 0, 0, 0}, dal[4] = {0, 0, 0, 0}, dam[4] = {0, 0, 0, 0};
+  const T ld = gl.d, md = gm.d;
+#pragma unroll
+  for (int corner = 0; corner < 4; ++corner) {
+    const bool hl = corner & 1, hm = corner & 2;
+    const int il = hl ? gl.i1 : gl.i0, im = hm ? gm.i1 : gm.i0;
+    const T fl = hl ? ld : T(1) - ld, fm = hm ? md : T(1) - md;
+    const T w = fl * fm, wl = (hl ? T(1) : T(-1)) * fm, wm = fl * (hm ? T(1) : T(-1));
+    const T* p = plane + kPlaneVals * (size_t(il) * mh + im);
+    Jones<T> e = jldg<T>(p);
+    const Cx<T>* e4 = &e.a;
+    Cx<T>* s4 = &sum.a; Cx<T>* l4 = &dsl.a; Cx<T>* m4 = &dsm.a;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const T ab = __ldg(p + 8 + k);
       s4[k] = s4[k] + e4[k] * w; amp[k] += w * ab;
       l4[k] = l4[k] + e4[k] * wl; dal[k] += wl * ab;
       m4[k] = m4[k] + e4[k] * wm; dam[k] += wm * ab;
@@ -846,7 +943,10 @@ __device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int c
     GridPos<T> gl = grid_pos<T>(l, A.ll, A.ul, A.lscale, A.lw);
     GridPos<T> gm = grid_pos<T>(m, A.lmm, A.um, A.mscale, A.mh);
     Jones<T> E, dEl, dEm;
-    beam_interp_d<T>(A.E_beam, G, gl, gm, cp, E, dEl, dEm);
+    if (A.plane)
+      beam_interp_plane_d<T>(A.plane + size_t(ch) * A.lw * A.mh * kPlaneVals, A.mh, gl, gm, E, dEl, dEm);
+    else
+      beam_interp_d<T>(A.E_beam, G, gl, gm, cp, E, dEl, dEm);
     const Jones<T>& B = src.B;
     Jones<T> KB = {cmul(K, B.a), cmul(K, B.b), cmul(K, B.c), cmul(K, B.d)};
     // E
@@ -904,7 +1004,7 @@ __device__ void adj_flush(const FusedArgs<T>& A, int t, int s0, int ns, T* sacc)
 }
 
 template <typename T, int RA, int RS>
-__global__ void __launch_bounds__(kFusedThreads) coh_adj_kernel(FusedArgs<T> A, SmemPlan S) {
+__global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<T> A, SmemPlan S) {
   extern __shared__ __align__(16) unsigned char smem[];
   AntInfo<T>* sa = reinterpret_cast<AntInfo<T>*>(smem + S.off_ant);
   SrcInfo<T>* ss = reinterpret_cast<SrcInfo<T>*>(smem + S.off_src);
@@ -953,6 +1053,47 @@ __global__ void __launch_bounds__(kFusedThreads) coh_adj_kernel(FusedArgs<T> A, 
 // ---------------------------------------------------------------------------
 // Small kernels: FP64 phase path lengths, gradient finalisation
 // ---------------------------------------------------------------------------
+// Frequency-blended beam plane per active channel (see beam_interp_plane).
+template <typename T>
+__global__ void beam_plane_kernel(FusedArgs<T> A, T* __restrict__ plane) {
+  const size_t cells = size_t(A.lw) * A.mh;
+  const size_t total = size_t(A.nchan) * cells;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+    const int ch = int(i / cells);
+    const size_t cell = i - size_t(ch) * cells;
+    const ChanPos<T> cp = chan_pos<T>(A.freq[ch], A.lfreq, A.ufreq, A.nud);
+    const T* e0 = A.E_beam + 8 * (cell * A.nud + cp.c0);
+    const T* e1 = A.E_beam + 8 * (cell * A.nud + cp.c1);
+    T* out = plane + kPlaneVals * i;
+    const T w0 = T(1) - cp.d, w1 = cp.d;
+    for (int k = 0; k < 4; ++k) {
+      const Cx<T> a{e0[2 * k], e0[2 * k + 1]}, b{e1[2 * k], e1[2 * k + 1]};
+      out[2 * k] = w0 * a.r + w1 * b.r;
+      out[2 * k + 1] = w0 * a.i + w1 * b.i;
+      out[8 + k] = w0 * cabs_(a) + w1 * cabs_(b);
+    }
+  }
+}
+
+// sqrt(B) at nu = nu_ref, and alpha / 2, per (source, time):
+// sqrt(B)(nu) = (nu / nu_ref)^(alpha / 2) * sqrt(B)(nu_ref).  Layout
+// [s][t][8] = ((I+Q+s0)/tau, (I-Q+s0)/tau, U/tau, V/tau, alpha/2, 0, 0, 0):
+// 32-byte entries, so the first four values are one aligned 16-byte load.
+template <typename T>
+__global__ void bsqrt_ref_kernel(FusedArgs<T> A, T* __restrict__ tab) {
+  const size_t total = size_t(A.nsrc) * A.ntime;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+    const int s = int(i / A.ntime), t = int(i % A.ntime);
+    const size_t st = size_t(s) * A.ltime + t;
+    const T* S = A.stokes + 4 * st;
+    const Jones<T> B = brightness_sqrt<T>(S[0], S[1], S[2], S[3], T(1));
+    T* o = tab + kBsqVals * i;
+    o[0] = B.a.r; o[1] = B.d.r; o[2] = B.b.r; o[3] = B.b.i;
+    o[4] = T(0.5) * A.alpha[st];
+    o[5] = o[6] = o[7] = T(0);
+  }
+}
+
 template <typename T>
 __global__ void phi_kernel(FusedArgs<T> A, double* __restrict__ phi) {
   size_t total = size_t(A.ntime) * A.nsrc * A.na;
@@ -1005,7 +1146,7 @@ __global__ void finalize_grads_kernel(FusedArgs<T> A, double scale, T* __restric
 // Host side
 // ---------------------------------------------------------------------------
 struct WsLayout {
-  size_t phi, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, err, total;
+  size_t phi, plane, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, err, total;
 };
 
 WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_grad) {
@@ -1016,6 +1157,8 @@ WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_gra
   size_t o = 0;
   auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 256); return r; };
   L.phi = take(nt * ns * na * 8);
+  L.plane = take(nc * size_t(d->beam_lw.local_size) * d->beam_mh.local_size * kPlaneVals * es);
+  L.bsq0 = take(dtype == MB_FLOAT32 ? ns * nt * kBsqVals * es : 0);
   L.partial = take(nt * nc * 8);
   L.gV = take(want_grad ? nt * nbl * nc * 8 * es : 0);
   L.dG = take(want_grad ? nt * na * nc * 8 * es : 0);
@@ -1060,10 +1203,13 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.model_vis = (T*)model_vis; A.chi2 = (T*)chi2;
   A.err = nullptr;
   A.phi = nullptr; A.partial = nullptr; A.gV = nullptr; A.dG = nullptr;
+  A.plane = nullptr; A.bsq0 = nullptr;
   A.acc_lm = A.acc_stokes = A.acc_alpha = A.acc_gauss = A.acc_sersic = nullptr;
   if (ws == nullptr) return MB_OK;
   char* w = static_cast<char*>(ws);
   A.phi = reinterpret_cast<const double*>(w + L.phi);
+  A.plane = reinterpret_cast<const T*>(w + L.plane);
+  A.bsq0 = sizeof(T) == 4 ? reinterpret_cast<const T*>(w + L.bsq0) : nullptr;
   A.partial = reinterpret_cast<double*>(w + L.partial);
   A.gV = want_grad ? reinterpret_cast<T*>(w + L.gV) : nullptr;
   A.dG = want_grad ? reinterpret_cast<T*>(w + L.dG) : nullptr;
@@ -1103,6 +1249,31 @@ mb_status check_inputs(const mb_dims* d, const mb_props* P, uint32_t options, co
   return MB_OK;
 }
 
+// Per-call tables shared by the forward and the adjoint: FP64 path lengths,
+// the frequency-blended beam plane, and (FP32) sqrt(B) at the reference
+// frequency.
+template <typename T>
+mb_status launch_prep(const FusedArgs<T>& A, void* ws, const WsLayout& L, cudaStream_t stream) {
+  char* w = static_cast<char*>(ws);
+  auto blocks_for = [](size_t n) { return int(std::min<size_t>((n + 255) / 256, 1u << 20)); };
+  size_t n = size_t(A.ntime) * A.nsrc * A.na;
+  if (n > 0) {
+    phi_kernel<T><<<blocks_for(n), 256, 0, stream>>>(A, reinterpret_cast<double*>(w + L.phi));
+    MB_CHECK(check_launch("phi_kernel"));
+  }
+  n = size_t(A.nchan) * A.lw * A.mh;
+  if (n > 0) {
+    beam_plane_kernel<T><<<blocks_for(n), 256, 0, stream>>>(A, reinterpret_cast<T*>(w + L.plane));
+    MB_CHECK(check_launch("beam_plane_kernel"));
+  }
+  n = size_t(A.nsrc) * A.ntime;
+  if (sizeof(T) == 4 && n > 0) {
+    bsqrt_ref_kernel<T><<<blocks_for(n), 256, 0, stream>>>(A, reinterpret_cast<T*>(w + L.bsq0));
+    MB_CHECK(check_launch("bsqrt_ref_kernel"));
+  }
+  return MB_OK;
+}
+
 mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2, cudaStream_t stream) {
   if (A.na > 64)
     return fail(MB_ERR_UNSUPPORTED, "split-precision modes handle up to 64 antennas (got %d)", A.na);
@@ -1117,7 +1288,7 @@ mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2,
   if (const char* g = getenv("MB_TC_GROUP")) P.group = std::max(1, atoi(g));
   // Stage buffers first (128-byte aligned), then the CUDA-core plan's regions,
   // shifted; the extended-source Jones tile reuses the stage buffers.
-  const size_t stage_bytes = size_t(kTcStages) * 2 * StageGeometry::kMatBytes;
+  const size_t stage_bytes = size_t(kTcStages) * 2 * StageGeometry<kTcRowBytes>::kMatBytes;
   const size_t need_J = sizeof(Jones<float>) * S.st * S.nap;
   const size_t stage_region = align_up(std::max(stage_bytes, need_J), 128);
   P.off_stage = 0;
@@ -1152,14 +1323,7 @@ mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* 
     MB_CUDA(cudaMemsetAsync(X2, 0, sizeof(double), stream));
     return MB_OK;
   }
-  {
-    size_t n = size_t(A.ntime) * A.nsrc * A.na;
-    if (n > 0) {
-      int blocks = int(std::min<size_t>((n + 255) / 256, 1u << 20));
-      phi_kernel<T><<<blocks, 256, 0, stream>>>(A, reinterpret_cast<double*>(static_cast<char*>(ws) + L.phi));
-      MB_CHECK(check_launch("phi_kernel"));
-    }
-  }
+  MB_CHECK(launch_prep(A, ws, L, stream));
   if constexpr (sizeof(T) == 4) {
     if (mode != MB_MODE_NATIVE) return launch_tc_forward(A, mode, X2, stream);
   }

@@ -28,6 +28,8 @@ struct FusedArgs {
   T* chi2;
   // workspace
   const double* phi;  // (ntime, nsrc, na) FP64 phase path lengths
+  const T* plane;     // (nchan, beam_lw, beam_mh, 12) frequency-blended beam, or NULL
+  const T* bsq0;      // (nsrc, ntime, 8) sqrt(B) at nu = nu_ref and alpha / 2, or NULL
   double* partial;    // (ntime * nchan) chi^2 partial sums
   T* gV;              // (ntime, nbl, nchan, 4) complex d chi^2 / d V
   T* dG;              // (ntime, na, nchan, 4) complex d chi^2 / d G
@@ -66,6 +68,7 @@ struct SmemPlan {
 };
 
 constexpr int kFusedThreads = 256;
+constexpr int kAdjThreads = 512;
 constexpr int kFwdMaxThreads = 320;
 
 size_t fused_workspace_size(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_grad);

@@ -17,7 +17,7 @@ template <int MODE>
 __global__ void __launch_bounds__(160) tc_selftest_kernel(const float* __restrict__ A, const float* __restrict__ B,
                                                           int K, float* __restrict__ D, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  using L = StageLayout<MODE>;
+  using L = StageLayout<MODE, 128>;
   unsigned char* sA_hi = smem;
   unsigned char* sA_lo = smem + L::kMatBytes;
   unsigned char* sB_hi = smem + 2 * L::kMatBytes;
@@ -92,12 +92,12 @@ mb_status mb_tc_selftest(const float* A, const float* B, int K, int mode, float*
   if (K <= 0 || K % kt != 0) return fail(MB_ERR_INVALID_ARG, "K must be a positive multiple of %d (got %d)", kt, K);
   cudaStream_t s = as_stream(stream);
   if (mode == MB_MODE_SPLIT_TF32) {
-    const size_t smem = 4 * StageLayout<MB_MODE_SPLIT_TF32>::kMatBytes;
+    const size_t smem = 4 * StageLayout<MB_MODE_SPLIT_TF32, 128>::kMatBytes;
     MB_CUDA(cudaFuncSetAttribute(tc_selftest_kernel<MB_MODE_SPLIT_TF32>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     tc_selftest_kernel<MB_MODE_SPLIT_TF32><<<1, 160, smem, s>>>(A, B, K, D, status);
   } else if (mode == MB_MODE_SPLIT_BF16) {
-    const size_t smem = 4 * StageLayout<MB_MODE_SPLIT_BF16>::kMatBytes;
+    const size_t smem = 4 * StageLayout<MB_MODE_SPLIT_BF16, 128>::kMatBytes;
     MB_CUDA(cudaFuncSetAttribute(tc_selftest_kernel<MB_MODE_SPLIT_BF16>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     tc_selftest_kernel<MB_MODE_SPLIT_BF16><<<1, 160, smem, s>>>(A, B, K, D, status);

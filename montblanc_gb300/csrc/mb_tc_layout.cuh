@@ -1,24 +1,27 @@
 // Shared-memory operand layout of one split-precision stage.
 //
-// An operand matrix has 128 rows (M or N) and 128 bytes of K per row
-// (32 TF32 or 64 BF16 values), stored in the tensor core's no-swizzle
-// K-major canonical layout: 8-row x 16-byte core matrices, core matrices
-// adjacent in K 128 bytes apart (LBO), 8-row groups 1024 bytes apart (SBO).
-// One MMA consumes 32 bytes of K (8 TF32 / 16 BF16), i.e. 2 core matrices,
-// so k-step kk starts kk * 256 bytes into the matrix.  A value x is stored
-// as hi + lo in two such matrices.
+// An operand matrix has 128 rows (M or N) and ROWB bytes of K per row
+// (ROWB / 4 TF32 or ROWB / 2 BF16 values), stored in the tensor core's
+// no-swizzle K-major canonical layout: 8-row x 16-byte core matrices, core
+// matrices adjacent in K 128 bytes apart (LBO), 8-row groups
+// (ROWB / 16) * 128 bytes apart (SBO).  One MMA consumes 32 bytes of K
+// (8 TF32 / 16 BF16), i.e. 2 core matrices, so k-step kk starts kk * 256
+// bytes into the matrix.  A value x is stored as hi + lo in two such
+// matrices.
 #pragma once
 
 #include "mb_tcgen05.cuh"
 
 namespace mb {
 
-template <int MODE> struct StageLayout;
+template <int MODE, int ROWB = 128> struct StageLayout;
 
+template <int ROWB>
 struct StageGeometry {
-  static constexpr int kRowBytes = 128;
-  static constexpr int kMatBytes = 128 * kRowBytes;  // 16 KB
-  static constexpr uint32_t kLBO = 128, kSBO = 1024;
+  static_assert(ROWB % 32 == 0, "a stage row holds whole MMA k-steps");
+  static constexpr int kRowBytes = ROWB;
+  static constexpr int kMatBytes = 128 * kRowBytes;
+  static constexpr uint32_t kLBO = 128, kSBO = (ROWB / 16) * 128;
   static constexpr int kKStepBytes = 256;
   static constexpr int kKSteps = kRowBytes / 32;
   __device__ __forceinline__ static uint32_t offset(int row, int kbyte) {
@@ -27,9 +30,10 @@ struct StageGeometry {
   __device__ __forceinline__ static uint64_t desc(uint32_t saddr) { return tc::smem_desc(saddr, kLBO, kSBO); }
 };
 
-template <> struct StageLayout<MB_MODE_SPLIT_TF32> : StageGeometry {
+template <int ROWB> struct StageLayout<MB_MODE_SPLIT_TF32, ROWB> : StageGeometry<ROWB> {
+  using G = StageGeometry<ROWB>;
   static constexpr int kElem = 4;
-  static constexpr int kKT = kRowBytes / kElem;  // 32 values of K per stage
+  static constexpr int kKT = ROWB / kElem;  // values of K per stage
   __host__ __device__ static constexpr uint32_t instr(uint32_t M, uint32_t N) { return tc::instr_desc(2, M, N); }
   __device__ __forceinline__ static void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
     tc::mma_tf32(d, a, b, id, acc);
@@ -37,7 +41,7 @@ template <> struct StageLayout<MB_MODE_SPLIT_TF32> : StageGeometry {
   __device__ __forceinline__ static void put(unsigned char* hi, unsigned char* lo, int row, int k, float x) {
     float h, l;
     tc::split_tf32(x, h, l);
-    const uint32_t o = offset(row, k * kElem);
+    const uint32_t o = G::offset(row, k * kElem);
     *reinterpret_cast<float*>(hi + o) = h;
     *reinterpret_cast<float*>(lo + o) = l;
   }
@@ -47,15 +51,16 @@ template <> struct StageLayout<MB_MODE_SPLIT_TF32> : StageGeometry {
     float h0, l0, h1, l1;
     tc::split_tf32(x0, h0, l0);
     tc::split_tf32(x1, h1, l1);
-    const uint32_t o = offset(row, k * kElem);
+    const uint32_t o = G::offset(row, k * kElem);
     *reinterpret_cast<float2*>(hi + o) = make_float2(h0, h1);
     *reinterpret_cast<float2*>(lo + o) = make_float2(l0, l1);
   }
 };
 
-template <> struct StageLayout<MB_MODE_SPLIT_BF16> : StageGeometry {
+template <int ROWB> struct StageLayout<MB_MODE_SPLIT_BF16, ROWB> : StageGeometry<ROWB> {
+  using G = StageGeometry<ROWB>;
   static constexpr int kElem = 2;
-  static constexpr int kKT = kRowBytes / kElem;  // 64 values of K per stage
+  static constexpr int kKT = ROWB / kElem;  // values of K per stage
   __host__ __device__ static constexpr uint32_t instr(uint32_t M, uint32_t N) { return tc::instr_desc(1, M, N); }
   __device__ __forceinline__ static void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
     tc::mma_f16(d, a, b, id, acc);
@@ -63,7 +68,7 @@ template <> struct StageLayout<MB_MODE_SPLIT_BF16> : StageGeometry {
   __device__ __forceinline__ static void put(unsigned char* hi, unsigned char* lo, int row, int k, float x) {
     __nv_bfloat16 h, l;
     tc::split_bf16(x, h, l);
-    const uint32_t o = offset(row, k * kElem);
+    const uint32_t o = G::offset(row, k * kElem);
     *reinterpret_cast<__nv_bfloat16*>(hi + o) = h;
     *reinterpret_cast<__nv_bfloat16*>(lo + o) = l;
   }
@@ -72,7 +77,7 @@ template <> struct StageLayout<MB_MODE_SPLIT_BF16> : StageGeometry {
     __nv_bfloat16 h0, l0, h1, l1;
     tc::split_bf16(x0, h0, l0);
     tc::split_bf16(x1, h1, l1);
-    const uint32_t o = offset(row, k * kElem);
+    const uint32_t o = G::offset(row, k * kElem);
     __nv_bfloat162 hh, ll;
     hh.x = h0; hh.y = h1; ll.x = l0; ll.y = l1;
     *reinterpret_cast<__nv_bfloat162*>(hi + o) = hh;

@@ -8,7 +8,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize('mode,K,tol', [('split_tf32', 32, 2e-6), ('split_tf32', 256, 2e-6),
+# One accumulator over all of K: the tensor core's FP32 accumulation rounds
+# toward zero, adding ~2.5e-8 relative per accumulation (3 per 8 TF32 / 16
+# BF16 values of K); BF16 hi + lo also has a ~5e-6 representation floor.
+@pytest.mark.parametrize('mode,K,tol', [('split_tf32', 32, 2e-6), ('split_tf32', 256, 5e-6),
                                         ('split_bf16', 64, 5e-5), ('split_bf16', 256, 5e-5)])
 def test_split_gemm_selftest(mode, K, tol):
     import torch

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 import golden_io
+from gpu_helpers import TOL
 
 pytestmark = pytest.mark.gpu
 
@@ -34,8 +35,12 @@ def _run(prob, fn, model_vis, chi2, x2):
     torch.cuda.synchronize()
 
 
-@pytest.mark.parametrize('dtype,tol', [('double', 1e-12), ('float', 1e-5)])
-def test_noalloc_matches_workspace_forward_twice(dtype, tol):
+@pytest.mark.parametrize('dtype', ['double', 'float'])
+def test_noalloc_matches_workspace_forward_twice(dtype):
+    # Same tolerances as the other parity tests: the allocation-free path
+    # forms the beam and phase terms without the workspace tables, so FP32
+    # results differ in rounding.
+    tol = TOL[dtype]
     import torch
     from montblanc_gb300.rime import RimeProblem
     problems = [RimeProblem.from_numpy(golden_io.load(n)[0], dtype=dtype)
@@ -48,9 +53,9 @@ def test_noalloc_matches_workspace_forward_twice(dtype, tol):
             v, c = prob.empty_vis(), prob.empty_chi2()
             x = torch.full((1,), float('nan'), dtype=torch.float64, device='cuda')
             _run(prob, 'noalloc', v, c, x)
-            assert golden_io.rel_err(v.cpu().numpy(), v_ref.cpu().numpy()) <= tol
-            assert golden_io.rel_err(c.cpu().numpy(), c_ref.cpu().numpy()) <= tol
-            assert abs(x.item() - x_ref.item()) <= tol * abs(x_ref.item())
+            assert golden_io.rel_err(v.cpu().numpy(), v_ref.cpu().numpy()) <= tol['vis']
+            assert golden_io.rel_err(c.cpu().numpy(), c_ref.cpu().numpy()) <= tol['terms']
+            assert abs(x.item() - x_ref.item()) <= tol['X2'] * abs(x_ref.item())
 
 
 def test_noalloc_rejects_too_many_units():
