@@ -38,8 +38,16 @@ template <typename T> struct FwdTile;
 template <> struct FwdTile<float> { static constexpr int RP = 2, RQ = 4, ST = 16; };
 template <> struct FwdTile<double> { static constexpr int RP = 1, RQ = 2, ST = 8; };
 template <typename T> struct AdjTile;
-template <> struct AdjTile<float> { static constexpr int RA = 2, RS = 2, ST = 32, THREADS = 512; };
-template <> struct AdjTile<double> { static constexpr int RA = 1, RS = 2, ST = 8, THREADS = 256; };
+// FULL_Y: the Hermitian matrix Y of d chi^2 / dV is kept complete (na x na
+// Jones) in shared memory; otherwise only its packed upper triangle.
+template <> struct AdjTile<float> {
+  static constexpr int RA = 2, RS = 4, ST = 16, THREADS = 512;
+  static constexpr bool FULL_Y = true;
+};
+template <> struct AdjTile<double> {
+  static constexpr int RA = 1, RS = 2, ST = 8, THREADS = 256;
+  static constexpr bool FULL_Y = false;
+};
 
 constexpr int kNAcc = 10;  // l, m, I, Q, U, V, alpha, shape0, shape1, shape2
 constexpr int kBsqVals = 8;  // values per (source, time) entry of the sqrt(B) table
@@ -75,7 +83,7 @@ SmemPlan make_plan(int na, bool adjoint) {
   S.off_src = take(sizeof(SrcInfo<T>) * S.st);
   S.off_J = take(sizeof(Jones<T>) * S.st * S.nap);
   S.off_gJ = take(adjoint ? sizeof(Jones<T>) * S.st * S.nap : 0);
-  S.off_V = take(sizeof(Jones<T>) * S.npairs);
+  S.off_V = take(sizeof(Jones<T>) * (adjoint && AdjTile<T>::FULL_Y ? size_t(na) * na : size_t(S.npairs)));
   // FP32 forward: low parts of float-float pair accumulators
   S.off_Vlo = take(!adjoint && sizeof(T) == 4 ? sizeof(Jones<T>) * S.npairs : 0);
   S.off_items = take(adjoint ? 0 : sizeof(int) * (S.nitems + 128));
@@ -112,35 +120,38 @@ __device__ __forceinline__ int src_type(const FusedArgs<T>& A, int s) {
   return s < A.npsrc ? SRC_POINT : (s < A.npsrc + A.ngsrc ? SRC_GAUSS : SRC_SERSIC);
 }
 
+// Per-source information of global source s at time t, channel ch.
+template <typename T>
+__device__ __forceinline__ SrcInfo<T> load_source_one(const FusedArgs<T>& A, int t, int ch, int s) {
+  const T f = A.freq[ch], rf = A.ref_freq[ch];
+  SrcInfo<T> si;
+  si.l = A.lm[2 * s]; si.m = A.lm[2 * s + 1];
+  {
+    const double l = si.l, m = si.m, nf = sqrt(1.0 - l * l - m * m);
+    si.l_over_n = T(l / nf);
+    si.m_over_n = T(m / nf);
+  }
+  size_t st = size_t(s) * A.ltime + t;
+  si.I = A.stokes[4 * st]; si.Q = A.stokes[4 * st + 1];
+  si.U = A.stokes[4 * st + 2]; si.V = A.stokes[4 * st + 3];
+  si.power = mb_pow(f / rf, A.alpha[st]);
+  si.B = brightness_sqrt<T>(si.I, si.Q, si.U, si.V, si.power);
+  si.type = src_type(A, s);
+  si.s0 = si.s1 = si.s2 = T(0);
+  if (si.type == SRC_GAUSS) {
+    int g = s - A.npsrc;
+    si.s0 = A.gauss[g]; si.s1 = A.gauss[A.lgsrc + g]; si.s2 = A.gauss[2 * A.lgsrc + g];
+  } else if (si.type == SRC_SERSIC) {
+    int x = s - A.npsrc - A.ngsrc;
+    si.s0 = A.sersic[x]; si.s1 = A.sersic[A.lssrc + x]; si.s2 = A.sersic[2 * A.lssrc + x];
+  }
+  return si;
+}
+
 // Per-source information of the tile [s0, s0 + ns) at time t, frequency f.
 template <typename T>
 __device__ void load_sources(const FusedArgs<T>& A, int t, int ch, int s0, int ns, SrcInfo<T>* ss) {
-  T f = A.freq[ch], rf = A.ref_freq[ch];
-  for (int i = threadIdx.x; i < ns; i += blockDim.x) {
-    int s = s0 + i;
-    SrcInfo<T> si;
-    si.l = A.lm[2 * s]; si.m = A.lm[2 * s + 1];
-    {
-      const double l = si.l, m = si.m, nf = sqrt(1.0 - l * l - m * m);
-      si.l_over_n = T(l / nf);
-      si.m_over_n = T(m / nf);
-    }
-    size_t st = size_t(s) * A.ltime + t;
-    si.I = A.stokes[4 * st]; si.Q = A.stokes[4 * st + 1];
-    si.U = A.stokes[4 * st + 2]; si.V = A.stokes[4 * st + 3];
-    si.power = mb_pow(f / rf, A.alpha[st]);
-    si.B = brightness_sqrt<T>(si.I, si.Q, si.U, si.V, si.power);
-    si.type = src_type(A, s);
-    si.s0 = si.s1 = si.s2 = T(0);
-    if (si.type == SRC_GAUSS) {
-      int g = s - A.npsrc;
-      si.s0 = A.gauss[g]; si.s1 = A.gauss[A.lgsrc + g]; si.s2 = A.gauss[2 * A.lgsrc + g];
-    } else if (si.type == SRC_SERSIC) {
-      int x = s - A.npsrc - A.ngsrc;
-      si.s0 = A.sersic[x]; si.s1 = A.sersic[A.lssrc + x]; si.s2 = A.sersic[2 * A.lssrc + x];
-    }
-    ss[i] = si;
-  }
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) ss[i] = load_source_one(A, t, ch, s0 + i);
 }
 
 template <typename T>
@@ -740,6 +751,74 @@ __device__ __forceinline__ Jones<T> y_entry(const Jones<T>* sX, int a, int b, in
   return jadd(x, jherm(x));
 }
 
+template <typename T>
+__device__ __forceinline__ Jones<T> y_at(const Jones<T>* sY, int a, int b, int na) {
+  if (AdjTile<T>::FULL_Y) return sY[a * na + b];
+  return y_entry(sY, a, b, na);
+}
+
+// dJ_a (s) = sum_b Y_ab J_b (s) for the point sources of a tile, with the
+// complete Y in shared memory.  Work item: 2 antennas x 4 sources x a
+// quarter of the b sum; the 4 quarters sit in adjacent lanes and are
+// combined with shuffles.
+template <typename T>
+__device__ void adj_consume_point_full(const FusedArgs<T>& A, const SmemPlan& S, int ns, const Jones<T>* sJ,
+                                       const Jones<T>* sY, Jones<T>* sgJ) {
+  constexpr int TA = 2, TS = 4, NB = 4;
+  const int nat = S.nap / TA, nsg = (S.st + TS - 1) / TS;
+  const int total = nat * nsg * NB;
+  const int rounds = (total + blockDim.x - 1) / blockDim.x;
+  for (int round = 0; round < rounds; ++round) {
+    const int k = round * blockDim.x + threadIdx.x;
+    const bool active = k < total;
+    const int bq = k & 3, rest = k >> 2;
+    const int at = rest % nat, sg = rest / nat;
+    const int a0 = at * TA, sb = sg * TS;
+    Jones<T> acc[TA][TS];
+#pragma unroll
+    for (int r = 0; r < TA; ++r)
+#pragma unroll
+      for (int c = 0; c < TS; ++c) acc[r][c] = jzero<T>();
+    if (active) {
+      for (int b = bq; b < A.na; b += NB) {
+        Jones<T> Y[TA], J[TS];
+#pragma unroll
+        for (int r = 0; r < TA; ++r)
+          Y[r] = (a0 + r < A.na) ? jload<T>(reinterpret_cast<const T*>(sY + (a0 + r) * A.na + b)) : jzero<T>();
+#pragma unroll
+        for (int c = 0; c < TS; ++c) {
+          const int si = min(sb + c, ns - 1);
+          J[c] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + b));
+        }
+#pragma unroll
+        for (int r = 0; r < TA; ++r)
+#pragma unroll
+          for (int c = 0; c < TS; ++c) jmac(acc[r][c], Y[r], J[c]);
+      }
+    }
+    // combine the 4 partial sums over b (all lanes take part)
+#pragma unroll
+    for (int r = 0; r < TA; ++r)
+#pragma unroll
+      for (int c = 0; c < TS; ++c) {
+        T* v = reinterpret_cast<T*>(&acc[r][c]);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          v[e] += __shfl_xor_sync(0xffffffffu, v[e], 1);
+          v[e] += __shfl_xor_sync(0xffffffffu, v[e], 2);
+        }
+      }
+    if (active) {
+      // lane bq writes outputs (r, c) with (r * TS + c) % NB == bq
+#pragma unroll
+      for (int r = 0; r < TA; ++r)
+#pragma unroll
+        for (int c = 0; c < TS; ++c)
+          if (((r * TS + c) & (NB - 1)) == bq && sb + c < ns) sgJ[(sb + c) * S.nap + a0 + r] = acc[r][c];
+    }
+  }
+}
+
 // Beam value and its derivatives with respect to the l and m grid offsets.
 template <typename T>
 __device__ void beam_interp_d(const T* __restrict__ E_beam, const BeamGeom& G, const GridPos<T>& gl,
@@ -905,7 +984,7 @@ __device__ void adj_consume_ext(const FusedArgs<T>& A, const SmemPlan& S, int ns
     Jones<T> acc = jzero<T>();
     T g0 = 0, g1 = 0, g2 = 0;
     for (int b = 0; b < A.na; ++b) {
-      Jones<T> Y = y_entry(sX, a, b, A.na);
+      Jones<T> Y = y_at(sX, a, b, A.na);
       Jones<T> P = jmul(Y, sJ[si * S.nap + b]);
       T d[3];
       T c = shape_and_grad<T>(src.type, sa[b].u - sa[a].u, sa[b].v - sa[a].v, src.s0, src.s1, src.s2, kg, ks, d);
@@ -922,6 +1001,58 @@ __device__ void adj_consume_ext(const FusedArgs<T>& A, const SmemPlan& S, int ns
   }
 }
 
+// Chain d chi^2 / dJ(s, a) through E, K and sqrt(B): the contributions to
+// d chi^2 / d(l, m, I, Q, U, V, alpha) of source s.
+template <typename T>
+__device__ __forceinline__ void chain_item(const FusedArgs<T>& A, int t, int ch, int s, int a, const SrcInfo<T>& src,
+                                           const AntInfo<T>& ai, const Jones<T>& gJ, T f, double nu_over_c,
+                                           T half_log_ratio, const ChanPos<T>& cp, T (&g)[7]) {
+  const double dphase = 2.0 * kPi * nu_over_c;  // |dK/dphi|
+  const BeamGeom G{A.lw, A.mh, A.nud};
+  Cx<T> K = phase_term(A, t, s, a, f, nu_over_c);
+  T l, m;
+  beam_lm<T>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
+  GridPos<T> gl = grid_pos<T>(l, A.ll, A.ul, A.lscale, A.lw);
+  GridPos<T> gm = grid_pos<T>(m, A.lmm, A.um, A.mscale, A.mh);
+  Jones<T> E, dEl, dEm;
+  if (A.plane)
+    beam_interp_plane_d<T>(A.plane + size_t(ch) * A.lw * A.mh * kPlaneVals, A.mh, gl, gm, E, dEl, dEm);
+  else
+    beam_interp_d<T>(A.E_beam, G, gl, gm, cp, E, dEl, dEm);
+  const Jones<T>& B = src.B;
+  Jones<T> KB = {cmul(K, B.a), cmul(K, B.b), cmul(K, B.c), cmul(K, B.d)};
+  // E
+  Jones<T> gE = jmulh(gJ, KB);
+  T g_ld = gl.inside ? jdot_re(gE, dEl) * A.lscale : T(0);
+  T g_md = gm.inside ? jdot_re(gE, dEm) * A.mscale : T(0);
+  T gl0 = g_ld * ai.sc_l * ai.cos_pa + g_md * ai.sc_m * ai.sin_pa;
+  T gm0 = -g_ld * ai.sc_l * ai.sin_pa + g_md * ai.sc_m * ai.cos_pa;
+  // K and sqrt(B)
+  Jones<T> gKB = jhmul(E, gJ);
+  Cx<T> gK = cmulc(gKB.a, B.a) + cmulc(gKB.b, B.b) + cmulc(gKB.c, B.c) + cmulc(gKB.d, B.d);
+  T gphi = T(dphase) * (gK.r * K.i - gK.i * K.r);
+  gl0 += gphi * (ai.u - ai.w * src.l_over_n);
+  gm0 += gphi * (ai.v - ai.w * src.m_over_n);
+  Cx<T> Kc = conj(K);
+  Jones<T> gB = {cmul(Kc, gKB.a), cmul(Kc, gKB.b), cmul(Kc, gKB.c), cmul(Kc, gKB.d)};
+  T GB = jdot_re(gB, B);
+  const T det0 = src.I * src.I - src.Q * src.Q - src.U * src.U - src.V * src.V;
+  const T s0v = mb_sqrt(det0 > T(0) ? det0 : T(0));
+  T gI = 0, gQ = 0, gU = 0, gVv = 0;
+  if (s0v > T(0)) {
+    T tt = mb_sqrt(T(2) * src.power * (src.I + s0v));
+    T pt = src.power / tt;
+    T tr1 = gB.a.r + gB.d.r;
+    T q2 = GB / (T(2) * s0v * (src.I + s0v));
+    gI = pt * (T(1) + src.I / s0v) * tr1 - GB / (T(2) * s0v);
+    gQ = pt * ((gB.a.r - gB.d.r) - (src.Q / s0v) * tr1) + q2 * src.Q;
+    gU = pt * ((gB.b.r + gB.c.r) - (src.U / s0v) * tr1) + q2 * src.U;
+    gVv = pt * ((gB.b.i - gB.c.i) - (src.V / s0v) * tr1) + q2 * src.V;
+  }
+  g[0] = gl0; g[1] = gm0; g[2] = gI; g[3] = gQ; g[4] = gU; g[5] = gVv;
+  g[6] = GB * half_log_ratio;
+}
+
 // Chain d chi^2 / dJ through E, K and sqrt(B) to the source parameters.
 template <typename T>
 __device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int ch, int s0, int ns,
@@ -929,59 +1060,14 @@ __device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int c
                           T* sacc, const ChanPos<T>& cp) {
   const T f = A.freq[ch];
   const double nu_over_c = double(f) / kLightSpeed;
-  const double dphase = 2.0 * kPi * nu_over_c;  // |dK/dphi|
   const T half_log_ratio = T(0.5) * mb_log(f / A.ref_freq[ch]);
-  const BeamGeom G{A.lw, A.mh, A.nud};
   for (int i = threadIdx.x; i < ns * A.na; i += blockDim.x) {
     const int si = i / A.na, a = i - si * A.na;
-    const SrcInfo<T>& src = ss[si];
-    const AntInfo<T>& ai = sa[a];
-    const Jones<T> gJ = sgJ[si * S.nap + a];
-    Cx<T> K = phase_term(A, t, s0 + si, a, f, nu_over_c);
-    T l, m;
-    beam_lm<T>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
-    GridPos<T> gl = grid_pos<T>(l, A.ll, A.ul, A.lscale, A.lw);
-    GridPos<T> gm = grid_pos<T>(m, A.lmm, A.um, A.mscale, A.mh);
-    Jones<T> E, dEl, dEm;
-    if (A.plane)
-      beam_interp_plane_d<T>(A.plane + size_t(ch) * A.lw * A.mh * kPlaneVals, A.mh, gl, gm, E, dEl, dEm);
-    else
-      beam_interp_d<T>(A.E_beam, G, gl, gm, cp, E, dEl, dEm);
-    const Jones<T>& B = src.B;
-    Jones<T> KB = {cmul(K, B.a), cmul(K, B.b), cmul(K, B.c), cmul(K, B.d)};
-    // E
-    Jones<T> gE = jmulh(gJ, KB);
-    T g_ld = gl.inside ? jdot_re(gE, dEl) * A.lscale : T(0);
-    T g_md = gm.inside ? jdot_re(gE, dEm) * A.mscale : T(0);
-    T gl0 = g_ld * ai.sc_l * ai.cos_pa + g_md * ai.sc_m * ai.sin_pa;
-    T gm0 = -g_ld * ai.sc_l * ai.sin_pa + g_md * ai.sc_m * ai.cos_pa;
-    // K and sqrt(B)
-    Jones<T> gKB = jhmul(E, gJ);
-    Cx<T> gK = cmulc(gKB.a, B.a) + cmulc(gKB.b, B.b) + cmulc(gKB.c, B.c) + cmulc(gKB.d, B.d);
-    T gphi = T(dphase) * (gK.r * K.i - gK.i * K.r);
-    gl0 += gphi * (ai.u - ai.w * src.l_over_n);
-    gm0 += gphi * (ai.v - ai.w * src.m_over_n);
-    Cx<T> Kc = conj(K);
-    Jones<T> gB = {cmul(Kc, gKB.a), cmul(Kc, gKB.b), cmul(Kc, gKB.c), cmul(Kc, gKB.d)};
-    T GB = jdot_re(gB, B);
-    const T det0 = src.I * src.I - src.Q * src.Q - src.U * src.U - src.V * src.V;
-    const T s0v = mb_sqrt(det0 > T(0) ? det0 : T(0));
-    T gI = 0, gQ = 0, gU = 0, gVv = 0;
-    if (s0v > T(0)) {
-      T tt = mb_sqrt(T(2) * src.power * (src.I + s0v));
-      T pt = src.power / tt;
-      T tr1 = gB.a.r + gB.d.r;
-      T q2 = GB / (T(2) * s0v * (src.I + s0v));
-      gI = pt * (T(1) + src.I / s0v) * tr1 - GB / (T(2) * s0v);
-      gQ = pt * ((gB.a.r - gB.d.r) - (src.Q / s0v) * tr1) + q2 * src.Q;
-      gU = pt * ((gB.b.r + gB.c.r) - (src.U / s0v) * tr1) + q2 * src.U;
-      gVv = pt * ((gB.b.i - gB.c.i) - (src.V / s0v) * tr1) + q2 * src.V;
-    }
-    T galpha = GB * half_log_ratio;
+    T g[7];
+    chain_item(A, t, ch, s0 + si, a, ss[si], sa[a], sgJ[si * S.nap + a], f, nu_over_c, half_log_ratio, cp, g);
     T* acc = sacc + si * kNAcc;
-    atomicAdd(acc + 0, gl0); atomicAdd(acc + 1, gm0);
-    atomicAdd(acc + 2, gI); atomicAdd(acc + 3, gQ); atomicAdd(acc + 4, gU); atomicAdd(acc + 5, gVv);
-    atomicAdd(acc + 6, galpha);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) atomicAdd(acc + k, g[k]);
   }
 }
 
@@ -1016,7 +1102,8 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
   const int unit = blockIdx.x;
   const int t = unit / A.nchan, ch = unit - t * A.nchan;
   load_antennas(A, t, ch, sa);
-  for (int i = threadIdx.x; i < S.npairs; i += blockDim.x) sX[i] = jzero<T>();
+  const int nx = AdjTile<T>::FULL_Y ? A.na * A.na : S.npairs;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) sX[i] = jzero<T>();
   for (int i = threadIdx.x; i < S.st * kNAcc; i += blockDim.x) sacc[i] = T(0);
   __syncthreads();
   for (int bl = threadIdx.x; bl < A.nbl; bl += blockDim.x) {
@@ -1024,22 +1111,32 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
     int p = A.ant1[tbl], q = A.ant2[tbl];
     if (p < 0 || p >= A.na || q < 0 || q >= A.na) continue;
     Jones<T> g = jload<T>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch));
-    if (p <= q) atomic_add_jones(&sX[pair_index(p, q, A.na)], g);
-    else atomic_add_jones(&sX[pair_index(q, p, A.na)], jherm(g));
+    if (AdjTile<T>::FULL_Y) {
+      // baseline (p, q): Y_pq += gV, Y_qp += gV^H (p == q: both terms)
+      atomic_add_jones(&sX[p * A.na + q], g);
+      atomic_add_jones(&sX[q * A.na + p], jherm(g));
+    } else if (p <= q) {
+      atomic_add_jones(&sX[pair_index(p, q, A.na)], g);
+    } else {
+      atomic_add_jones(&sX[pair_index(q, p, A.na)], jherm(g));
+    }
   }
   __syncthreads();
 
   const T f = A.freq[ch];
   const ChanPos<T> cp = chan_pos<T>(f, A.lfreq, A.ufreq, A.nud);
   const T kg = A.gauss_scale * f, ks = A.two_pi_over_c * f;
-  for (int s0 = 0; s0 < A.nsrc;) {
+  for (int s0 = A.sbeg; s0 < A.nsrc;) {
     int s1 = s0 < A.npsrc ? min(s0 + S.st, A.npsrc) : min(s0 + S.st, A.nsrc);
     int ns = s1 - s0;
     load_sources(A, t, ch, s0, ns, ss);
     __syncthreads();
     produce_jones(A, S, t, ch, s0, ns, ss, sa, sJ, cp);
     __syncthreads();
-    if (s0 < A.npsrc) adj_consume_point<T, RA, RS>(A, S, ns, sJ, sX, sgJ);
+    if (s0 < A.npsrc) {
+      if (AdjTile<T>::FULL_Y) adj_consume_point_full<T>(A, S, ns, sJ, sX, sgJ);
+      else adj_consume_point<T, RA, RS>(A, S, ns, sJ, sX, sgJ);
+    }
     else adj_consume_ext<T>(A, S, ns, ss, sa, sJ, sX, sgJ, sacc, kg, ks);
     __syncthreads();
     adj_chain<T>(A, S, t, ch, s0, ns, ss, sa, sgJ, sacc, cp);
@@ -1048,6 +1145,303 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
     __syncthreads();
     s0 = s1;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Split-precision adjoint: dJ = Y J for point sources on the tensor cores
+// ---------------------------------------------------------------------------
+// Y (2na x 2na complex, rows (a, i), columns (b, j)) is the Hermitian matrix
+// of d chi^2 / dV.  As a real operand (128 rows x 256 K, BF16 hi + lo):
+//   Yop[(a,i), (b,j)] = Re Y_ab[i][j],  Yop[(a,i), 128 + (b,j)] = -Im Y_ab[i][j].
+// Per tile of kTaKappa sources the producers stage
+//   Jop[(s,k), (b,j)] = Re J_sb[j][k],  Jop[(s,k), 128 + (b,j)] = Im J_sb[j][k]
+// and one MMA warp forms, in TMEM,
+//   D_re = Yop Jop^T                          = Re (Y J)
+//   D_im = (-Yop_im) Jop_re^T + Yop_re Jop_im^T = Im (Y J)
+// (the second with the instruction's negate-A bit), each operand as
+// hi.hi + hi.lo + lo.hi.  Chain warps read dJ(s, a) straight from TMEM.
+constexpr int kTaRowBytes = 512;      // 256 BF16 values of K per operand row
+constexpr int kTaKappa = 8;           // sources per tile (16 operand rows)
+constexpr int kTaStages = 3;
+constexpr int kTaProducers = 128;     // warps 0-3
+constexpr int kTaChain = 256;         // warps 4-11
+constexpr int kTaThreads = kTaProducers + kTaChain + 32;  // warp 12: MMA
+constexpr uint32_t kTaCols = 64;      // 2 buffers x (D_re 16 + D_im 16)
+using TaGeom = StageGeometry<kTaRowBytes>;
+using TaLayout = StageLayout<MB_MODE_SPLIT_BF16, kTaRowBytes>;
+constexpr size_t kYopBytes = 2 * size_t(TaGeom::kMatBytes);          // hi + lo: 128 KB
+constexpr size_t kJopBytes = 2 * size_t(2 * 8 * kTaRowBytes);       // hi + lo, 16 rows
+
+// Y of one (time, channel) unit from d chi^2 / dV, written as the BF16
+// hi + lo tensor-core operand above (A_hi at +0, A_lo at +64 KB).
+__global__ void yop_build_kernel(FusedArgs<float> A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Jones<float>* sY = reinterpret_cast<Jones<float>*>(smem);
+  const int unit = blockIdx.x;
+  const int t = unit / A.nchan, ch = unit - t * A.nchan;
+  const int na = A.na;
+  for (int i = threadIdx.x; i < na * na; i += blockDim.x) sY[i] = jzero<float>();
+  __syncthreads();
+  for (int bl = threadIdx.x; bl < A.nbl; bl += blockDim.x) {
+    const size_t tbl = size_t(t) * A.lnbl + bl;
+    const int p = A.ant1[tbl], q = A.ant2[tbl];
+    if (p < 0 || p >= na || q < 0 || q >= na) continue;
+    const Jones<float> g = jload<float>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch));
+    atomic_add_jones(&sY[p * na + q], g);
+    atomic_add_jones(&sY[q * na + p], jherm(g));
+  }
+  __syncthreads();
+  unsigned char* hi = A.yop + size_t(unit) * kYopBytes;
+  unsigned char* lo = hi + TaGeom::kMatBytes;
+  // element pairs (row r, K = 2kp, 2kp + 1): j = 0, 1 of antenna b
+  for (int idx = threadIdx.x; idx < 128 * 128; idx += blockDim.x) {
+    const int r = idx >> 7, kp = idx & 127;
+    const int a = r >> 1, i = r & 1;
+    const bool im = kp >= 64;
+    const int b = im ? kp - 64 : kp;
+    float x0 = 0.f, x1 = 0.f;
+    if (a < na && b < na) {
+      const Jones<float> y = sY[a * na + b];
+      const Cx<float> y0 = i ? y.c : y.a, y1 = i ? y.d : y.b;  // Y_ab[i][0], Y_ab[i][1]
+      x0 = im ? -y0.i : y0.r;
+      x1 = im ? -y1.i : y1.r;
+    }
+    __nv_bfloat16 h0, l0, h1, l1;
+    tc::split_bf16(x0, h0, l0);
+    tc::split_bf16(x1, h1, l1);
+    const uint32_t o = TaGeom::offset(r, 2 * (2 * kp));
+    __nv_bfloat162 hh, ll;
+    hh.x = h0; hh.y = h1; ll.x = l0; ll.y = l1;
+    *reinterpret_cast<__nv_bfloat162*>(hi + o) = hh;
+    *reinterpret_cast<__nv_bfloat162*>(lo + o) = ll;
+  }
+}
+
+__device__ __forceinline__ bool named_sync_chain_or(bool x) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, 2, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"(uint32_t(x)), "n"(kTaChain)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ void named_sync_chain() {
+  asm volatile("bar.sync 2, %0;" ::"n"(kTaChain) : "memory");
+}
+
+struct TaPlan {
+  size_t off_yop, off_stage, off_ant, off_acc, off_bar, total;
+};
+
+__global__ void __launch_bounds__(kTaThreads) coh_tc_adj_kernel(FusedArgs<float> A, TaPlan P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned char* syop = smem + P.off_yop;
+  unsigned char* stage = smem + P.off_stage;
+  AntInfo<float>* sa = reinterpret_cast<AntInfo<float>*>(smem + P.off_ant);
+  float* sacc = reinterpret_cast<float*>(smem + P.off_acc);  // [kTaKappa][7]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + P.off_bar);
+  uint64_t* full = bars;                    // [kTaStages]
+  uint64_t* empty = bars + kTaStages;       // [kTaStages]
+  uint64_t* dfull = bars + 2 * kTaStages;   // [2] MMA -> chain
+  uint64_t* dfree = dfull + 2;              // [2] chain -> MMA
+  uint64_t* done = dfree + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int unit = blockIdx.x;
+  const int t = unit / A.nchan, ch = unit - t * A.nchan;
+  if (tid == 0) *abort_flag = A.err ? *reinterpret_cast<volatile int*>(A.err) : 0;
+  __syncthreads();
+  if (*abort_flag) return;
+  __syncthreads();
+
+  // Y operand of this unit: 128 KB, 16-byte vector copies
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(A.yop + size_t(unit) * kYopBytes);
+    uint4* dst = reinterpret_cast<uint4*>(syop);
+    for (int i = tid; i < int(kYopBytes / 16); i += blockDim.x) dst[i] = __ldg(src + i);
+  }
+  load_antennas(A, t, ch, sa);
+  for (int i = tid; i < kTaKappa * 7; i += blockDim.x) sacc[i] = 0.f;
+  if (tid == 0) {
+    for (int i = 0; i < kTaStages; ++i) {
+      tc::mbar_init(full + i, kTaProducers);
+      tc::mbar_init(empty + i, 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(dfull + i, 1);
+      tc::mbar_init(dfree + i, kTaChain);
+    }
+    tc::mbar_init(done, 1);
+  }
+  tc::fence_proxy_async_smem();
+  if (warp == 12) tc::tmem_alloc(tmem_slot, kTaCols);
+  tc::fence_before_thread_sync();
+  __syncthreads();
+  tc::fence_after_thread_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  const float f = A.freq[ch];
+  const double nu_over_c = double(f) / kLightSpeed;
+  const ChanPos<float> cp = chan_pos<float>(f, A.lfreq, A.ufreq, A.nud);
+  const float log2_ratio = log2f(f / A.ref_freq[ch]);
+  const float half_log_ratio = 0.5f * logf(f / A.ref_freq[ch]);
+  const int ntiles = (A.npsrc + kTaKappa - 1) / kTaKappa;
+
+  if (warp < 4) {
+    // ---- producers: J of the tile's (source, antenna) pairs into Jop ------
+    bool bad = false;
+    for (int g = 0; g < ntiles && !bad; ++g) {
+      const int slot = g % kTaStages, use = g / kTaStages;
+      if (!tc::mbar_wait(empty + slot, (use & 1) ^ 1)) { bad = true; break; }
+      const int s0 = g * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
+      unsigned char* hi = stage + size_t(slot) * kJopBytes;
+      unsigned char* lo = hi + kJopBytes / 2;
+#pragma unroll 1
+      for (int rep = 0; rep < 4; ++rep) {
+        // warp w, rep: antennas 4 (w + 4 rep) + (lane & 3), source lane >> 2
+        const int b = 4 * (warp + 4 * rep) + (lane & 3), sl = lane >> 2;
+        Jones<float> J = jzero<float>();
+        if (b < A.na && sl < ns) {
+          const SrcInfo<float> src = point_source_info(A, t, ch, s0 + sl, log2_ratio);
+          J = compute_jones(A, t, s0 + sl, b, src, sa[b], f, nu_over_c, cp, ch);
+        }
+        // row (s, k): K = (b, 0), (b, 1) hold J[0][k], J[1][k]
+        TaLayout::put2(hi, lo, 2 * sl, 2 * b, J.a.r, J.c.r);
+        TaLayout::put2(hi, lo, 2 * sl, 128 + 2 * b, J.a.i, J.c.i);
+        TaLayout::put2(hi, lo, 2 * sl + 1, 2 * b, J.b.r, J.d.r);
+        TaLayout::put2(hi, lo, 2 * sl + 1, 128 + 2 * b, J.b.i, J.d.i);
+      }
+      tc::fence_proxy_async_smem();
+      tc::mbar_arrive(full + slot);
+    }
+    if (bad) *abort_flag = 1;
+  } else if (warp < 12) {
+    // ---- chain warps: dJ from TMEM, chain to source parameters ------------
+    const int c = warp - 4, q = c & 3, set = c >> 2;
+    const int r = 32 * q + lane, a = r >> 1, i = r & 1;
+    const int base = 4 * set;               // the warp's 4 sources of a tile
+    bool bad = false;
+    for (int g = 0; g < ntiles; ++g) {
+      const int buf = g & 1;
+      if (!bad) bad = !tc::mbar_wait(dfull + buf, (g >> 1) & 1);
+      tc::fence_after_thread_sync();
+      float v[32];
+      tc::tmem_ld32(tmem + (uint32_t(32 * q) << 16) + uint32_t(32 * buf), v);
+      tc::fence_before_thread_sync();
+      tc::mbar_arrive(dfree + buf);
+      // own row i of dJ for the set's 4 sources; the partner lane holds row 1-i
+      // give the partner the sources it chains: lane i=0 chains base+0,1,
+      // lane i=1 chains base+2,3
+      float give[8], recv[8];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int sl = base + (i ? u : 2 + u);
+        give[4 * u + 0] = v[2 * sl];      give[4 * u + 1] = v[2 * sl + 1];
+        give[4 * u + 2] = v[16 + 2 * sl]; give[4 * u + 3] = v[16 + 2 * sl + 1];
+      }
+#pragma unroll
+      for (int e = 0; e < 8; ++e) recv[e] = __shfl_xor_sync(0xffffffffu, give[e], 1);
+      float gsum[2][7];
+      const int s0 = g * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int sl = base + 2 * i + u;
+        // rows of dJ: own row i from v, the other from recv
+        const Cx<float> o0{v[2 * sl], v[16 + 2 * sl]}, o1{v[2 * sl + 1], v[16 + 2 * sl + 1]};
+        const Cx<float> p0{recv[4 * u], recv[4 * u + 2]}, p1{recv[4 * u + 1], recv[4 * u + 3]};
+        Jones<float> gJ;
+        gJ.a = i ? p0 : o0; gJ.b = i ? p1 : o1;
+        gJ.c = i ? o0 : p0; gJ.d = i ? o1 : p1;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) gsum[u][k] = 0.f;
+        if (!bad && a < A.na && sl < ns) {
+          const SrcInfo<float> src = load_source_one(A, t, ch, s0 + sl);
+          chain_item(A, t, ch, s0 + sl, a, src, sa[a], gJ, f, nu_over_c, half_log_ratio, cp, gsum[u]);
+        }
+      }
+      // sum over the warp's 16 antennas (lane bits 1-4), then into shared memory
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+          float x = gsum[u][k];
+          x += __shfl_xor_sync(0xffffffffu, x, 2);
+          x += __shfl_xor_sync(0xffffffffu, x, 4);
+          x += __shfl_xor_sync(0xffffffffu, x, 8);
+          x += __shfl_xor_sync(0xffffffffu, x, 16);
+          if (lane < 2) atomicAdd(sacc + (base + 2 * i + u) * 7 + k, x);
+        }
+      if (named_sync_chain_or(bad)) { bad = true; break; }
+      // flush the tile's per-source sums to the FP64 accumulators
+      const int ct = tid - 4 * 32;
+      if (ct < kTaKappa * 7) {
+        const int sl = ct / 7, k = ct - sl * 7, sg = s0 + sl;
+        const double val = double(sacc[ct]);
+        sacc[ct] = 0.f;
+        if (sl < ns && val != 0.0) {
+          if (k < 2) atomicAdd(&A.acc_lm[2 * sg + k], val);
+          else if (k < 6) atomicAdd(&A.acc_stokes[(size_t(sg) * A.ntime + t) * 4 + (k - 2)], val);
+          else atomicAdd(&A.acc_alpha[size_t(sg) * A.ntime + t], val);
+        }
+      }
+      named_sync_chain();
+    }
+    if (bad && c == 0 && lane == 0) *abort_flag = 1;
+  } else if (lane == 0) {
+    // ---- MMA issue ---------------------------------------------------------
+    const uint32_t idesc = TaLayout::instr(128, 16);
+    const uint32_t idesc_neg = idesc | (1u << 13);  // negate A
+    const uint32_t yhi = tc::smem_addr(syop), ylo = yhi + TaGeom::kMatBytes;
+    bool issued = false, bad = false;
+    for (int g = 0; g < ntiles; ++g) {
+      const int slot = g % kTaStages, use = g / kTaStages, buf = g & 1;
+      if (!tc::mbar_wait(full + slot, use & 1)) { bad = true; break; }
+      if (g >= 2 && !tc::mbar_wait(dfree + buf, ((g >> 1) - 1) & 1)) { bad = true; break; }
+      tc::fence_after_thread_sync();
+      const uint32_t jhi = tc::smem_addr(stage + size_t(slot) * kJopBytes), jlo = jhi + kJopBytes / 2;
+      const uint32_t dre = tmem + uint32_t(32 * buf), dim = dre + 16;
+#pragma unroll 1
+      for (int kk = 0; kk < TaGeom::kKSteps; ++kk) {
+        const uint32_t o = kk * TaGeom::kKStepBytes;
+        const uint64_t ah = TaGeom::desc(yhi + o), al = TaGeom::desc(ylo + o);
+        const uint64_t bh = TaGeom::desc(jhi + o), bl = TaGeom::desc(jlo + o);
+        TaLayout::mma(dre, ah, bh, idesc, kk == 0 ? 0u : 1u);
+        TaLayout::mma(dre, ah, bl, idesc, 1u);
+        TaLayout::mma(dre, al, bh, idesc, 1u);
+      }
+      const int half = TaGeom::kKSteps / 2;
+#pragma unroll 1
+      for (int kk = 0; kk < half; ++kk) {
+        const uint32_t ore = kk * TaGeom::kKStepBytes, oim = (kk + half) * TaGeom::kKStepBytes;
+        // D_im += (-Y_im) J_re
+        TaLayout::mma(dim, TaGeom::desc(yhi + oim), TaGeom::desc(jhi + ore), idesc_neg, kk == 0 ? 0u : 1u);
+        TaLayout::mma(dim, TaGeom::desc(yhi + oim), TaGeom::desc(jlo + ore), idesc_neg, 1u);
+        TaLayout::mma(dim, TaGeom::desc(ylo + oim), TaGeom::desc(jhi + ore), idesc_neg, 1u);
+        // D_im += Y_re J_im
+        TaLayout::mma(dim, TaGeom::desc(yhi + ore), TaGeom::desc(jhi + oim), idesc, 1u);
+        TaLayout::mma(dim, TaGeom::desc(yhi + ore), TaGeom::desc(jlo + oim), idesc, 1u);
+        TaLayout::mma(dim, TaGeom::desc(ylo + ore), TaGeom::desc(jhi + oim), idesc, 1u);
+      }
+      issued = true;
+      tc::mma_commit(empty + slot);
+      tc::mma_commit(dfull + buf);
+    }
+    if (issued) {
+      tc::mma_commit(done);
+      if (!tc::mbar_wait(done, 0)) bad = true;
+    }
+    if (bad) *abort_flag = 1;
+  }
+  tc::fence_before_thread_sync();
+  __syncthreads();
+  tc::fence_after_thread_sync();
+  if (warp == 12) tc::tmem_dealloc(tmem, kTaCols);
+  if (*abort_flag && tid == 0 && A.err) atomicExch(A.err, int(MB_ERR_TIMEOUT));
 }
 
 // ---------------------------------------------------------------------------
@@ -1146,7 +1540,8 @@ __global__ void finalize_grads_kernel(FusedArgs<T> A, double scale, T* __restric
 // Host side
 // ---------------------------------------------------------------------------
 struct WsLayout {
-  size_t phi, plane, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, err, total;
+  size_t phi, plane, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, err, yop,
+      total;
 };
 
 WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_grad) {
@@ -1169,6 +1564,7 @@ WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_gra
   L.acc_sersic = take(want_grad ? 3 * nx * 8 : 0);
   L.acc_end = o;
   L.err = take(sizeof(int));
+  L.yop = take(want_grad && mode != MB_MODE_NATIVE && dtype == MB_FLOAT32 ? nt * nc * kYopBytes : 0);
   L.total = o;
   return L;
 }
@@ -1182,7 +1578,7 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.ltime = d->ntime.local_size; A.lna = d->na.local_size; A.lnbl = d->nbl.local_size;
   A.lchan = d->nchan.local_size; A.lgsrc = d->ngsrc.local_size; A.lssrc = d->nssrc.local_size;
   A.lw = d->beam_lw.local_size; A.mh = d->beam_mh.local_size; A.nud = d->beam_nud.local_size;
-  A.t0 = 0; A.ch0 = 0;
+  A.t0 = 0; A.ch0 = 0; A.sbeg = 0;
   A.accumulate_in = d->nsrc.lower_extent > 0;
   A.partial_out = d->nsrc.upper_extent < d->nsrc.global_size;
   A.weights = options & MB_APPLY_WEIGHTS;
@@ -1203,7 +1599,7 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.model_vis = (T*)model_vis; A.chi2 = (T*)chi2;
   A.err = nullptr;
   A.phi = nullptr; A.partial = nullptr; A.gV = nullptr; A.dG = nullptr;
-  A.plane = nullptr; A.bsq0 = nullptr;
+  A.plane = nullptr; A.bsq0 = nullptr; A.yop = nullptr;
   A.acc_lm = A.acc_stokes = A.acc_alpha = A.acc_gauss = A.acc_sersic = nullptr;
   if (ws == nullptr) return MB_OK;
   char* w = static_cast<char*>(ws);
@@ -1219,6 +1615,7 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.acc_gauss = reinterpret_cast<double*>(w + L.acc_gauss);
   A.acc_sersic = reinterpret_cast<double*>(w + L.acc_sersic);
   A.err = reinterpret_cast<int*>(w + L.err);
+  A.yop = (want_grad && L.yop != L.total) ? reinterpret_cast<unsigned char*>(w + L.yop) : nullptr;
   return MB_OK;
 }
 
@@ -1342,13 +1739,57 @@ mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* 
   return check_launch("sum_partials_kernel");
 }
 
+// Split-precision adjoint: Y operands, point sources on the tensor cores,
+// extended sources on the CUDA cores (same FP64 accumulators).
+mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
+  if (A.na > 64)
+    return fail(MB_ERR_UNSUPPORTED, "split-precision modes handle up to 64 antennas (got %d)", A.na);
+  if (A.yop == nullptr) return fail(MB_ERR_WORKSPACE, "workspace lacks the adjoint operand region");
+  const int units = A.ntime * A.nchan;
+  if (A.err) MB_CUDA(cudaMemsetAsync(A.err, 0, sizeof(int), stream));
+  if (A.npsrc > 0) {
+    const size_t ysmem = size_t(A.na) * A.na * sizeof(Jones<float>);
+    MB_CUDA(cudaFuncSetAttribute(yop_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(ysmem)));
+    yop_build_kernel<<<units, 256, ysmem, stream>>>(A);
+    MB_CHECK(check_launch("yop_build_kernel"));
+    TaPlan P;
+    size_t o = 0;
+    auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 128); return r; };
+    P.off_yop = take(kYopBytes);
+    P.off_stage = take(size_t(kTaStages) * kJopBytes);
+    P.off_ant = take(sizeof(AntInfo<float>) * A.na);
+    P.off_acc = take(sizeof(float) * kTaKappa * 7);
+    P.off_bar = take((2 * kTaStages + 5) * sizeof(uint64_t) + 16);
+    P.total = o;
+    MB_CUDA(cudaFuncSetAttribute(coh_tc_adj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
+    coh_tc_adj_kernel<<<units, kTaThreads, P.total, stream>>>(A, P);
+    MB_CHECK(check_launch("coh_tc_adj_kernel"));
+  }
+  if (A.nsrc > A.npsrc) {
+    A.sbeg = A.npsrc;
+    SmemPlan S = make_plan<float>(A.na, true);
+    auto kern = coh_adj_kernel<float, AdjTile<float>::RA, AdjTile<float>::RS>;
+    MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
+    kern<<<units, S.nthreads, S.total, stream>>>(A, S);
+    MB_CHECK(check_launch("coh_adj_kernel"));
+  }
+  return MB_OK;
+}
+
 template <typename T>
-mb_status launch_adjoint(const FusedArgs<T>& A, double grad_scale, const mb_rime_grads* g, void* ws,
-                         const WsLayout& L, cudaStream_t stream) {
+mb_status launch_adjoint(const FusedArgs<T>& A, mb_mode mode, double grad_scale, const mb_rime_grads* g,
+                         void* ws, const WsLayout& L, cudaStream_t stream) {
   char* w = static_cast<char*>(ws);
   MB_CUDA(cudaMemsetAsync(w + L.acc_lm, 0, L.acc_end - L.acc_lm, stream));
   const int units = A.ntime * A.nchan;
-  if (units > 0 && A.nsrc > 0) {
+  bool done_sources = false;
+  if constexpr (sizeof(T) == 4) {
+    if (mode != MB_MODE_NATIVE && units > 0 && A.nsrc > 0) {
+      MB_CHECK(launch_tc_adjoint(A, stream));
+      done_sources = true;
+    }
+  }
+  if (units > 0 && A.nsrc > 0 && !done_sources) {
     constexpr int RA = AdjTile<T>::RA, RS = AdjTile<T>::RS;
     SmemPlan S = make_plan<T>(A.na, true);
     if (S.total > 227 * 1024)
@@ -1490,11 +1931,11 @@ mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims, con
   if (dtype == MB_FLOAT32) {
     FusedArgs<float> A;
     fill_args(A, dims, props, options, in, nullptr, nullptr, true, workspace, L);
-    return launch_adjoint(A, grad_scale, grads, workspace, L, s);
+    return launch_adjoint(A, mode, grad_scale, grads, workspace, L, s);
   }
   FusedArgs<double> A;
   fill_args(A, dims, props, options, in, nullptr, nullptr, true, workspace, L);
-  return launch_adjoint(A, grad_scale, grads, workspace, L, s);
+  return launch_adjoint(A, mode, grad_scale, grads, workspace, L, s);
 }
 
 }  // extern "C"

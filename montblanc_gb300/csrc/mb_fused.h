@@ -15,6 +15,7 @@ struct FusedArgs {
   int ltime, lna, lnbl, lchan, lgsrc, lssrc;
   int lw, mh, nud;
   int t0, ch0;  // first (time, channel) unit handled by this launch
+  int sbeg;     // first source handled by the CUDA-core adjoint
   bool accumulate_in, partial_out, weights, residuals, want_grad;
   T ll, lmm, ul, um, lfreq, ufreq, lscale, mscale, gauss_scale, two_pi_over_c;
   double inv_sigma2;
@@ -36,6 +37,7 @@ struct FusedArgs {
   // adjoint accumulators (FP64)
   double *acc_lm, *acc_stokes, *acc_alpha, *acc_gauss, *acc_sersic;
   int* err;  // device error word (bounded waits that gave up), or NULL
+  unsigned char* yop;  // (ntime * nchan) x 128 KB tensor-core operands of d chi^2 / dV, or NULL
 };
 
 // Per-antenna data for one (time, channel) unit.

@@ -117,3 +117,23 @@ def test_gradient_finite_differences_medium_workload():
         checked += abs(num) > 10 * fd_noise
     # most of the 50 draws must be far enough above the FD floor to count
     assert checked >= 25, checked
+
+
+@pytest.mark.parametrize('mode', ['split_tf32', 'split_bf16'])
+@pytest.mark.parametrize('seed,use_w,mix', [(51, True, (5, 3, 2)), (52, False, (7, 0, 0)),
+                                            (53, True, (0, 2, 2))])
+def test_split_adjoint_matches_numpy_gradient(mode, seed, use_w, mix):
+    """Point-source dJ = Y J on the tensor cores (BF16 hi + lo operands),
+    extended sources on the CUDA cores, against the FP64 NumPy gradient."""
+    from montblanc_gb300.rime import RimeProblem
+    np_, ng, ns = mix
+    P = small_problem(seed, use_w, np_=np_, ng=ng, ns=ns, offset=2e-4)
+    chi2, ref = OA.chi2_grad(P)
+    prob = RimeProblem.from_numpy(P, dtype='float')
+    x2, g = prob.chi2_and_grad(mode=mode)
+    assert abs(x2.item() - chi2) <= 1e-4 * abs(chi2)
+    for k in PARAMS:
+        if ref[k].size == 0:
+            continue
+        err = grad_err(g[k].cpu().numpy(), ref[k])
+        assert err < 2e-3, (k, err)
