@@ -48,6 +48,49 @@ SM_COUNT = 152
 NCU_TRAFFIC = {}
 
 
+def workload_terms(name):
+    """(point-source terms, extended-source terms) of one chi^2 evaluation."""
+    from montblanc_gb300 import synth
+    w = synth.WORKLOADS[name]
+    vis = w['ntime'] * synth.nr_of_baselines(w['na']) * w['nchan']
+    return w['npsrc'] * vis, (w['ngsrc'] + w['nssrc']) * vis
+
+
+def roofline(workload, mode, kernels, peak, peak_src, clk):
+    """Roofline of the kernel with the largest share of the timed steps.
+
+    achieved = algorithmic flops per launch / mean CUDA-event duration of
+    that kernel's launches in the timed region (events on its launch
+    stream).  Algorithmic flops: FLOPS_FWD per source.vis term for the
+    forward coherency kernels, FLOPS_ADJ per term for the adjoint kernels,
+    over the sources each kernel handles (split modes: the tensor-core
+    kernels take the point sources; the CUDA-core adjoint the rest)."""
+    pt, et = workload_terms(workload)
+    split = mode != 'native'
+    work = {
+        'coh_tc_fwd_kernel': FLOPS_FWD * (pt + et),
+        'coh_fwd_kernel': FLOPS_FWD * (pt + et),
+        'coh_tc_adj_kernel': FLOPS_ADJ * pt,
+        'coh_adj_kernel': FLOPS_ADJ * (et if split else pt + et),
+    }
+    name = max(kernels, key=lambda k: kernels[k][0])
+    ms, n = kernels[name]
+    per_launch_ms = ms / n
+    flops = work.get(name)
+    sm_mhz = clk.get('sm_mhz') or 2070.0
+    fp32_peak = SM_COUNT * 128 * 2 * sm_mhz * 1e6 / 1e12
+    out = {'bound': 'tensor', 'kernel': name, 'launch_ms': per_launch_ms, 'unit': 'TFLOP/s',
+           'peak': peak, 'peak_source': '%s bf16 sustained (MEASURED_PEAKS.json)' % peak_src,
+           'traffic': NCU_TRAFFIC.get((name, workload, mode))}
+    if flops is None:
+        out.update({'achieved': None, 'frac': None})
+        return out
+    achieved = flops / (per_launch_ms * 1e-3) / 1e12
+    out.update({'achieved': achieved, 'frac': achieved / peak, 'algorithmic_flops_per_launch': flops,
+                'fp32_simt_peak_tflops_at_clock': fp32_peak, 'fp32_simt_frac': achieved / fp32_peak})
+    return out
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -55,8 +98,8 @@ def parse():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     ap.add_argument('--workload', default='large_point')
-    ap.add_argument('--mode', default='native', help="native | split_tf32 | split_bf16")
-    ap.add_argument('--compare-plain', action='store_true', help='also time the plain FP32 form')
+    ap.add_argument('--mode', default='split_tf32', help="native | split_tf32 | split_bf16")
+    ap.add_argument('--no-plain', action='store_true', help='skip timing the plain FP32 CUDA-core form')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--seed', type=int, default=20261203)
@@ -245,9 +288,14 @@ def errors_vs_fp64(P, prob, mode):
 # ---------------------------------------------------------------------------
 # timing
 # ---------------------------------------------------------------------------
-def time_resident(prob, mode, steps, warmup, ws):
-    """Device-resident chi^2 + gradient; returns (ms/step, fwd ms, adj ms)."""
+def time_resident(prob, mode, steps, warmup, ws, kernels=None):
+    """Device-resident chi^2 + gradient; returns (ms/step, fwd ms, adj ms).
+
+    With ``kernels`` (a dict), the library's per-kernel CUDA-event times of
+    the timed steps are stored in it, {name: (total ms, launches)}, and the
+    number of library launches under the key '_launches'."""
     import torch
+    from montblanc_gb300 import _cabi
     stream = torch.cuda.current_stream()
     grads = prob.empty_grads()
 
@@ -267,15 +315,37 @@ def time_resident(prob, mode, steps, warmup, ws):
     barrier(ws)
     torch.cuda.synchronize()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
-    for i in range(steps):
-        step(evs[i])
-    torch.cuda.synchronize()
+    with _cabi.KernelTimer() as kt:
+        for i in range(steps):
+            step(evs[i])
+        torch.cuda.synchronize()
     barrier(ws)
     torch.cuda.synchronize()
+    if kernels is not None:
+        kernels.update(kt.times())
+        kernels['_launches'] = kt.launches
     total = evs[0][0].elapsed_time(evs[-1][2])
     fwd = [e[0].elapsed_time(e[1]) for e in evs]
     adj = [e[1].elapsed_time(e[2]) for e in evs]
     return total / steps, statistics.mean(fwd), statistics.mean(adj)
+
+
+def time_plain_slice(P, prob, ws, ntime=20):
+    import numpy as np
+    import torch
+    from montblanc_gb300.rime import RimeProblem
+    nt = min(ntime, prob.ntime)
+    Q = subset_problem(P, prob, list(range(nt)), list(range(prob.nchan)))
+    sub = RimeProblem.from_numpy(Q, dtype='float')
+    terms = prob.nsrc * nt * prob.nbl * prob.nchan
+    ms, fwd, adj = time_resident(sub, 'native', 1, 1, ws)
+    ms = max_over_ranks(ws, ms)
+    out = {'value': ws * terms / (ms * 1e-3), 'unit': UNIT, 'ms_per_step': ms, 'forward_ms': fwd,
+           'adjoint_ms': adj, 'mode': 'native',
+           'sample': 'first %d of %d time steps, all sources, baselines and channels' % (nt, prob.ntime)}
+    del sub
+    torch.cuda.empty_cache()
+    return out
 
 
 def time_e2e(prob, mode, steps, warmup, ws):
@@ -391,17 +461,17 @@ def main():
 
     clocks = Clocks()
     clocks.start()
-    ms, fwd_ms, adj_ms = time_resident(prob, args.mode, args.steps, args.warmup, ws)
+    kernels = {}
+    ms, fwd_ms, adj_ms = time_resident(prob, args.mode, args.steps, args.warmup, ws, kernels)
     clk = clocks.stop()
     ms_max = max_over_ranks(ws, ms)
     value = ws * terms / (ms_max * 1e-3)
 
     plain = None
-    if args.compare_plain and args.mode != 'native':
-        pms, _, _ = time_resident(prob, 'native', args.steps, 1, ws)
-        pms = max_over_ranks(ws, pms)
-        plain = {'value': ws * terms / (pms * 1e-3), 'ms_per_step': pms, 'mode': 'native'}
-
+    if not args.no_plain and args.mode != 'native':
+        # The plain FP32 CUDA-core form on the first 20 time steps of the same
+        # workload (throughput per term does not depend on the time extent).
+        plain = time_plain_slice(P, prob, ws)
     e2e = None
     if not args.no_e2e:
         ems, h2d, d2h = time_e2e(prob, args.mode, args.steps, 1, ws)
@@ -413,12 +483,8 @@ def main():
         return
     errs = errors_vs_fp64(P, prob, args.mode)
     burst, sustained, hbm, src = peaks()
-    dominant = 'coh_adj_kernel' if adj_ms >= fwd_ms else 'coh_fwd_kernel'
-    dom_ms = max(adj_ms, fwd_ms)
-    dom_flops = (FLOPS_ADJ if dominant == 'coh_adj_kernel' else FLOPS_FWD) * terms
-    achieved = dom_flops / (dom_ms * 1e-3) / 1e12
-    sm_mhz = clk.get('sm_mhz') or 2070.0
-    fp32_peak = SM_COUNT * 128 * 2 * sm_mhz * 1e6 / 1e12
+    launches = kernels.pop('_launches')
+    rl = roofline(args.workload, args.mode, kernels, sustained, src, clk)
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms_max, 'higher_is_better': True, 'scaling': 'weak',
@@ -429,19 +495,15 @@ def main():
                          % (prob.arrays['observed_vis'].numel() * 8 / 1e9),
                    'phase': 'FP64 argument and range reduction', 'replicas': ws},
         'forward_ms': fwd_ms, 'adjoint_ms': adj_ms,
-        'roofline': {'bound': 'tensor', 'kernel': dominant, 'achieved': achieved, 'peak': sustained,
-                     'unit': 'TFLOP/s', 'frac': achieved / sustained,
-                     'peak_source': '%s bf16 sustained (MEASURED_PEAKS.json)' % src,
-                     'traffic': NCU_TRAFFIC.get((dominant, args.workload)),
-                     'algorithmic_flops_per_launch': dom_flops,
-                     'fp32_simt_peak_tflops_at_clock': fp32_peak,
-                     'fp32_simt_frac': achieved / fp32_peak},
+        'roofline': rl,
+        'kernels_ms_per_step': {k: v[0] / args.steps for k, v in sorted(kernels.items())},
         'errors_vs_fp64': errs,
-        'gpu_launches': 5 * args.steps + (args.steps if args.mode != 'native' else 0),
+        'gpu_launches': launches,
         'clocks': clk,
     }
     if plain:
         line['plain_fp32'] = plain
+        line['split_over_plain'] = value / plain['value']
     if e2e:
         line['e2e'] = e2e
     if not args.no_cpu:

@@ -225,6 +225,22 @@ mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
 mb_status mb_tc_selftest(const float* A, const float* B, int K, int mode,
                          float* D, int* status, void* stream);
 
+/* Diagnostics, no counterpart in the reference: launch accounting and
+ * per-kernel CUDA-event timing of this library's kernels.
+ * mb_kernel_launches: kernels launched by the library in this process.
+ * mb_kernel_timing(1) starts recording a CUDA event pair on the launch
+ * stream around every launch (0 stops; recorded events are kept).
+ * mb_kernel_time: total milliseconds and launch count of the recorded
+ * launches whose kernel name equals `name` (NULL: all); synchronises on
+ * the recorded events.  mb_kernel_timing_reset drops the records. */
+uint64_t mb_kernel_launches(void);
+mb_status mb_kernel_timing(int enable);
+mb_status mb_kernel_time(const char* name, double* total_ms, int64_t* launches);
+mb_status mb_kernel_timing_reset(void);
+/* Name of the i-th distinct kernel timed since the process started (NULL
+ * past the end); the returned string stays valid for the process. */
+const char* mb_kernel_timing_name(int i);
+
 /* ------------------------------------------------------------------------
  * Allocation-free forward.  No counterpart in the reference.
  *

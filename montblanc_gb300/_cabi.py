@@ -83,6 +83,11 @@ SIGNATURES = {
     'mb_rime_noalloc_max_units': (_sz, []),
     'mb_rime_forward_noalloc': (_i32, [_i32, _pdims, _pprops, _u32, ctypes.POINTER(MbRimeInputs), _vp, _vp,
                                        _vp, _vp]),
+    'mb_kernel_launches': (ctypes.c_uint64, []),
+    'mb_kernel_timing': (_i32, [_i32]),
+    'mb_kernel_time': (_i32, [ctypes.c_char_p, ctypes.POINTER(_dbl), ctypes.POINTER(ctypes.c_int64)]),
+    'mb_kernel_timing_reset': (_i32, []),
+    'mb_kernel_timing_name': (ctypes.c_char_p, [_i32]),
 }
 
 
@@ -135,6 +140,46 @@ def make_props(**kw):
 
 def version():
     return lib.mb_version().decode()
+
+
+def kernel_launches():
+    """Kernels this library has launched in this process."""
+    return int(lib.mb_kernel_launches())
+
+
+class KernelTimer:
+    """Per-kernel CUDA-event timing of the library's launches while active.
+
+    ``with KernelTimer() as kt: ...`` records an event pair on the launch
+    stream around every launch inside the block; ``kt.times()`` maps each
+    kernel name to (total ms, launches) and ``kt.launches`` is the number of
+    launches the block made.
+    """
+
+    def __enter__(self):
+        call('mb_kernel_timing_reset')
+        self._n0 = kernel_launches()
+        call('mb_kernel_timing', 1)
+        return self
+
+    def __exit__(self, *exc):
+        call('mb_kernel_timing', 0)
+        self.launches = kernel_launches() - self._n0
+        return False
+
+    def times(self):
+        out = {}
+        i = 0
+        while True:
+            name = lib.mb_kernel_timing_name(i)
+            if name is None:
+                break
+            ms, n = ctypes.c_double(), ctypes.c_int64()
+            call('mb_kernel_time', name, ctypes.byref(ms), ctypes.byref(n))
+            if n.value:
+                out[name.decode()] = (ms.value, n.value)
+            i += 1
+        return out
 
 
 def exported_symbols():

@@ -1,6 +1,10 @@
 // Library-wide C-ABI pieces: version, thread-local error state and
 // dimension validation.
+#include <atomic>
 #include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
 
 #include "mb_internal.h"
 
@@ -48,9 +52,97 @@ mb_status check_dims(const mb_dims* d, bool need_beam) {
   return MB_OK;
 }
 
+// ---- launch accounting and per-kernel timing ---------------------------------
+namespace {
+
+struct TimedLaunch {
+  const char* name;  // static string of the launch site
+  cudaEvent_t start, stop;
+};
+
+std::atomic<uint64_t> g_launches{0};
+std::atomic<bool> g_timing{false};
+std::mutex g_timing_mutex;
+std::vector<TimedLaunch> g_records;
+std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_free_events;
+std::vector<std::string> g_names;
+
+}  // namespace
+
+KernelScope::KernelScope(const char* name, cudaStream_t stream) : slot_(-1), stream_(stream) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  if (!g_timing.load(std::memory_order_relaxed)) return;
+  std::lock_guard<std::mutex> lock(g_timing_mutex);
+  std::pair<cudaEvent_t, cudaEvent_t> ev;
+  if (!g_free_events.empty()) {
+    ev = g_free_events.back();
+    g_free_events.pop_back();
+  } else if (cudaEventCreate(&ev.first) != cudaSuccess || cudaEventCreate(&ev.second) != cudaSuccess) {
+    return;  // timing is best-effort; the launch itself proceeds
+  }
+  if (cudaEventRecord(ev.first, stream) != cudaSuccess) {
+    g_free_events.push_back(ev);
+    return;
+  }
+  slot_ = int(g_records.size());
+  g_records.push_back({name, ev.first, ev.second});
+}
+
+KernelScope::~KernelScope() {
+  if (slot_ < 0) return;
+  std::lock_guard<std::mutex> lock(g_timing_mutex);
+  if (slot_ < int(g_records.size())) cudaEventRecord(g_records[slot_].stop, stream_);
+}
+
 }  // namespace mb
 
 extern "C" {
+
+uint64_t mb_kernel_launches(void) { return mb::g_launches.load(); }
+
+mb_status mb_kernel_timing(int enable) {
+  mb::g_timing.store(enable != 0);
+  return MB_OK;
+}
+
+mb_status mb_kernel_time(const char* name, double* total_ms, int64_t* launches) {
+  MB_REQUIRE(total_ms, "total_ms");
+  MB_REQUIRE(launches, "launches");
+  std::lock_guard<std::mutex> lock(mb::g_timing_mutex);
+  double ms = 0.0;
+  int64_t n = 0;
+  for (const auto& r : mb::g_records) {
+    if (name != nullptr && std::strcmp(name, r.name) != 0) continue;
+    MB_CUDA(cudaEventSynchronize(r.stop));
+    float e = 0.f;
+    MB_CUDA(cudaEventElapsedTime(&e, r.start, r.stop));
+    ms += e;
+    ++n;
+  }
+  *total_ms = ms;
+  *launches = n;
+  return MB_OK;
+}
+
+mb_status mb_kernel_timing_reset(void) {
+  std::lock_guard<std::mutex> lock(mb::g_timing_mutex);
+  for (const auto& r : mb::g_records) {
+    MB_CUDA(cudaEventSynchronize(r.stop));
+    mb::g_free_events.push_back({r.start, r.stop});
+  }
+  mb::g_records.clear();
+  return MB_OK;
+}
+
+const char* mb_kernel_timing_name(int i) {
+  std::lock_guard<std::mutex> lock(mb::g_timing_mutex);
+  for (const auto& r : mb::g_records) {
+    bool seen = false;
+    for (const auto& x : mb::g_names) seen = seen || x == r.name;
+    if (!seen) mb::g_names.push_back(r.name);
+  }
+  return (i >= 0 && i < int(mb::g_names.size())) ? mb::g_names[i].c_str() : nullptr;
+}
 
 const char* mb_version(void) { return "montblanc_gb300 0.1 (sm_103a)"; }
 

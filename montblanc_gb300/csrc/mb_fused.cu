@@ -1655,17 +1655,26 @@ mb_status launch_prep(const FusedArgs<T>& A, void* ws, const WsLayout& L, cudaSt
   auto blocks_for = [](size_t n) { return int(std::min<size_t>((n + 255) / 256, 1u << 20)); };
   size_t n = size_t(A.ntime) * A.nsrc * A.na;
   if (n > 0) {
-    phi_kernel<T><<<blocks_for(n), 256, 0, stream>>>(A, reinterpret_cast<double*>(w + L.phi));
+    {
+      KernelScope ks_("phi_kernel", stream);
+      phi_kernel<T><<<blocks_for(n), 256, 0, stream>>>(A, reinterpret_cast<double*>(w + L.phi));
+    }
     MB_CHECK(check_launch("phi_kernel"));
   }
   n = size_t(A.nchan) * A.lw * A.mh;
   if (n > 0) {
-    beam_plane_kernel<T><<<blocks_for(n), 256, 0, stream>>>(A, reinterpret_cast<T*>(w + L.plane));
+    {
+      KernelScope ks_("beam_plane_kernel", stream);
+      beam_plane_kernel<T><<<blocks_for(n), 256, 0, stream>>>(A, reinterpret_cast<T*>(w + L.plane));
+    }
     MB_CHECK(check_launch("beam_plane_kernel"));
   }
   n = size_t(A.nsrc) * A.ntime;
   if (sizeof(T) == 4 && n > 0) {
-    bsqrt_ref_kernel<T><<<blocks_for(n), 256, 0, stream>>>(A, reinterpret_cast<T*>(w + L.bsq0));
+    {
+      KernelScope ks_("bsqrt_ref_kernel", stream);
+      bsqrt_ref_kernel<T><<<blocks_for(n), 256, 0, stream>>>(A, reinterpret_cast<T*>(w + L.bsq0));
+    }
     MB_CHECK(check_launch("bsqrt_ref_kernel"));
   }
   return MB_OK;
@@ -1701,14 +1710,17 @@ mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2,
   if (mode == MB_MODE_SPLIT_TF32) {
     auto kern = coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
-    kern<<<units, kTcThreads, P.total, stream>>>(A, S, P);
+    { KernelScope ks_("coh_tc_fwd_kernel", stream); kern<<<units, kTcThreads, P.total, stream>>>(A, S, P); }
   } else {
     auto kern = coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
-    kern<<<units, kTcThreads, P.total, stream>>>(A, S, P);
+    { KernelScope ks_("coh_tc_fwd_kernel", stream); kern<<<units, kTcThreads, P.total, stream>>>(A, S, P); }
   }
   MB_CHECK(check_launch("coh_tc_fwd_kernel"));
-  sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, A.weights ? 1.0 : A.inv_sigma2, X2);
+  {
+    KernelScope ks_("sum_partials_kernel", stream);
+    sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, A.weights ? 1.0 : A.inv_sigma2, X2);
+  }
   return check_launch("sum_partials_kernel");
 }
 
@@ -1732,10 +1744,13 @@ mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* 
                 S.total, A.na);
   auto kern = coh_fwd_kernel<T, RP, RQ>;
   MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
-  kern<<<units, S.nthreads, S.total, stream>>>(B, S);
+  { KernelScope ks_("coh_fwd_kernel", stream); kern<<<units, S.nthreads, S.total, stream>>>(B, S); }
   MB_CHECK(check_launch("coh_fwd_kernel"));
   const double scale = A.weights ? 1.0 : A.inv_sigma2;
-  sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, scale, X2);
+  {
+    KernelScope ks_("sum_partials_kernel", stream);
+    sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, scale, X2);
+  }
   return check_launch("sum_partials_kernel");
 }
 
@@ -1750,7 +1765,7 @@ mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
   if (A.npsrc > 0) {
     const size_t ysmem = size_t(A.na) * A.na * sizeof(Jones<float>);
     MB_CUDA(cudaFuncSetAttribute(yop_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(ysmem)));
-    yop_build_kernel<<<units, 256, ysmem, stream>>>(A);
+    { KernelScope ks_("yop_build_kernel", stream); yop_build_kernel<<<units, 256, ysmem, stream>>>(A); }
     MB_CHECK(check_launch("yop_build_kernel"));
     TaPlan P;
     size_t o = 0;
@@ -1762,7 +1777,10 @@ mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
     P.off_bar = take((2 * kTaStages + 5) * sizeof(uint64_t) + 16);
     P.total = o;
     MB_CUDA(cudaFuncSetAttribute(coh_tc_adj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
-    coh_tc_adj_kernel<<<units, kTaThreads, P.total, stream>>>(A, P);
+    {
+      KernelScope ks_("coh_tc_adj_kernel", stream);
+      coh_tc_adj_kernel<<<units, kTaThreads, P.total, stream>>>(A, P);
+    }
     MB_CHECK(check_launch("coh_tc_adj_kernel"));
   }
   if (A.nsrc > A.npsrc) {
@@ -1770,7 +1788,7 @@ mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
     SmemPlan S = make_plan<float>(A.na, true);
     auto kern = coh_adj_kernel<float, AdjTile<float>::RA, AdjTile<float>::RS>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
-    kern<<<units, S.nthreads, S.total, stream>>>(A, S);
+    { KernelScope ks_("coh_adj_kernel", stream); kern<<<units, S.nthreads, S.total, stream>>>(A, S); }
     MB_CHECK(check_launch("coh_adj_kernel"));
   }
   return MB_OK;
@@ -1796,15 +1814,18 @@ mb_status launch_adjoint(const FusedArgs<T>& A, mb_mode mode, double grad_scale,
       return fail(MB_ERR_UNSUPPORTED, "fused adjoint needs %zu bytes of shared memory for na=%d", S.total, A.na);
     auto kern = coh_adj_kernel<T, RA, RS>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
-    kern<<<units, S.nthreads, S.total, stream>>>(A, S);
+    { KernelScope ks_("coh_adj_kernel", stream); kern<<<units, S.nthreads, S.total, stream>>>(A, S); }
     MB_CHECK(check_launch("coh_adj_kernel"));
   }
   size_t total = size_t(A.nsrc) * 2 + size_t(A.nsrc) * A.ntime + 3 * size_t(A.ngsrc) + 3 * size_t(A.nssrc) +
                  size_t(A.ntime) * A.na * A.nchan;
   if (total > 0) {
     int blocks = int(std::min<size_t>((total + 255) / 256, 1u << 16));
-    finalize_grads_kernel<T><<<blocks, 256, 0, stream>>>(A, grad_scale, (T*)g->lm, (T*)g->stokes, (T*)g->alpha,
-                                                         (T*)g->gauss_shape, (T*)g->sersic_shape, (T*)g->G_term);
+    {
+      KernelScope ks_("finalize_grads_kernel", stream);
+      finalize_grads_kernel<T><<<blocks, 256, 0, stream>>>(A, grad_scale, (T*)g->lm, (T*)g->stokes, (T*)g->alpha,
+                                                           (T*)g->gauss_shape, (T*)g->sersic_shape, (T*)g->G_term);
+    }
     MB_CHECK(check_launch("finalize_grads_kernel"));
   }
   return MB_OK;
@@ -1859,7 +1880,10 @@ mb_status launch_forward_noalloc(FusedArgs<T> A, double* partials, double* X2, c
   A.want_grad = false;
   const int units = A.ntime * A.nchan;
   if (units == 0) {
-    sum_partials_kernel<<<1, 1024, 0, stream>>>(partials, 0, 1.0, X2);
+    {
+      KernelScope ks_("sum_partials_kernel", stream);
+      sum_partials_kernel<<<1, 1024, 0, stream>>>(partials, 0, 1.0, X2);
+    }
     return check_launch("sum_partials_kernel");
   }
   constexpr int RP = FwdTile<T>::RP, RQ = FwdTile<T>::RQ;
@@ -1869,9 +1893,12 @@ mb_status launch_forward_noalloc(FusedArgs<T> A, double* partials, double* X2, c
                 S.total, A.na);
   auto kern = coh_fwd_kernel<T, RP, RQ>;
   MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
-  kern<<<units, S.nthreads, S.total, stream>>>(A, S);
+  { KernelScope ks_("coh_fwd_kernel", stream); kern<<<units, S.nthreads, S.total, stream>>>(A, S); }
   MB_CHECK(check_launch("coh_fwd_kernel"));
-  sum_partials_kernel<<<1, 1024, 0, stream>>>(partials, units, A.weights ? 1.0 : A.inv_sigma2, X2);
+  {
+    KernelScope ks_("sum_partials_kernel", stream);
+    sum_partials_kernel<<<1, 1024, 0, stream>>>(partials, units, A.weights ? 1.0 : A.inv_sigma2, X2);
+  }
   return check_launch("sum_partials_kernel");
 }
 }  // namespace

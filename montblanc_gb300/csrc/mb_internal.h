@@ -51,6 +51,21 @@ inline mb_status check_launch(const char* what) {
       return ::mb::fail(MB_ERR_CUDA, "%s: %s", #expr, cudaGetErrorString(_e)); \
   } while (0)
 
+// Launch accounting around one kernel launch: counts every launch of this
+// library and, while per-kernel timing is switched on, records a CUDA event
+// pair on the launch stream (read back by mb_kernel_time).
+class KernelScope {
+ public:
+  KernelScope(const char* name, cudaStream_t stream);
+  ~KernelScope();
+  KernelScope(const KernelScope&) = delete;
+  KernelScope& operator=(const KernelScope&) = delete;
+
+ private:
+  int slot_;
+  cudaStream_t stream_;
+};
+
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Arrays read with vector loads must be aligned: complex Jones arrays to

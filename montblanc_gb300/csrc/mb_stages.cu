@@ -268,13 +268,15 @@ mb_status mb_bsqrt(mb_dtype dtype, const mb_dims* dims, const void* stokes, cons
   size_t n = size_t(D.nsrc) * D.ntime * D.nchan;
   if (n == 0) return MB_OK;
   cudaStream_t s = as_stream(stream);
-  if (dtype == MB_FLOAT32)
+  if (dtype == MB_FLOAT32) {
+    KernelScope ks_("bsqrt_kernel", s);
     bsqrt_kernel<float><<<grid_for(n), kThreads, 0, s>>>(D, (const float*)stokes, (const float*)alpha,
         (const float*)frequency, (const float*)ref_frequency, (float*)B_sqrt);
-  else if (dtype == MB_FLOAT64)
+  } else if (dtype == MB_FLOAT64) {
+    KernelScope ks_("bsqrt_kernel", s);
     bsqrt_kernel<double><<<grid_for(n), kThreads, 0, s>>>(D, (const double*)stokes, (const double*)alpha,
         (const double*)frequency, (const double*)ref_frequency, (double*)B_sqrt);
-  else return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
+  } else return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
   return check_launch("mb_bsqrt");
 }
 
@@ -290,15 +292,17 @@ mb_status mb_ebeam(mb_dtype dtype, const mb_dims* dims, const mb_props* props, c
   size_t n = size_t(D.ntime) * D.na * D.nchan;
   if (n == 0 || D.nsrc == 0) return MB_OK;
   cudaStream_t s = as_stream(stream);
-  if (dtype == MB_FLOAT32)
+  if (dtype == MB_FLOAT32) {
+    KernelScope ks_("ebeam_kernel", s);
     ebeam_kernel<float><<<grid_for(n), kThreads, 0, s>>>(D, *props, (const float*)lm,
         (const float*)parallactic_angles, (const float*)point_errors, (const float*)antenna_scaling,
         (const float*)frequency, (const float*)E_beam, (float*)jones);
-  else if (dtype == MB_FLOAT64)
+  } else if (dtype == MB_FLOAT64) {
+    KernelScope ks_("ebeam_kernel", s);
     ebeam_kernel<double><<<grid_for(n), kThreads, 0, s>>>(D, *props, (const double*)lm,
         (const double*)parallactic_angles, (const double*)point_errors, (const double*)antenna_scaling,
         (const double*)frequency, (const double*)E_beam, (double*)jones);
-  else return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
+  } else return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
   return check_launch("mb_ebeam");
 }
 
@@ -312,13 +316,15 @@ mb_status mb_ekb_sqrt(mb_dtype dtype, const mb_dims* dims, const mb_props* props
   size_t n = size_t(D.ntime) * D.na * D.nchan;
   if (n == 0 || D.nsrc == 0) return MB_OK;
   cudaStream_t s = as_stream(stream);
-  if (dtype == MB_FLOAT32)
+  if (dtype == MB_FLOAT32) {
+    KernelScope ks_("ekb_kernel", s);
     ekb_kernel<float><<<grid_for(n), kThreads, 0, s>>>(D, (const float*)uvw, (const float*)lm,
         (const float*)frequency, (const float*)B_sqrt, (float*)jones);
-  else if (dtype == MB_FLOAT64)
+  } else if (dtype == MB_FLOAT64) {
+    KernelScope ks_("ekb_kernel", s);
     ekb_kernel<double><<<grid_for(n), kThreads, 0, s>>>(D, (const double*)uvw, (const double*)lm,
         (const double*)frequency, (const double*)B_sqrt, (double*)jones);
-  else return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
+  } else return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
   return check_launch("mb_ekb_sqrt");
 }
 
@@ -347,10 +353,14 @@ mb_status mb_sum_coherencies(mb_dtype dtype, const mb_dims* dims, const mb_props
   if (n == 0) return MB_OK;
   cudaStream_t s = as_stream(stream);
   const bool w = options & MB_APPLY_WEIGHTS, r = options & MB_RESIDUALS;
-#define MB_SUMCOH(T, W, R)                                                                          \
-  sumcoh_kernel<T, W, R><<<grid_for(n), kThreads, 0, s>>>(D, *props, (const T*)uvw, (const T*)gauss_shape, \
-      (const T*)sersic_shape, (const T*)frequency, antenna1, antenna2, (const T*)jones, flag,          \
-      (const T*)weight_vector, (const T*)observed_vis, (const T*)G_term, (T*)model_vis, (T*)chi_sqrd_result)
+#define MB_SUMCOH(T, W, R)                                                                               \
+  do {                                                                                                 \
+    KernelScope ks_("sumcoh_kernel", s);                                                               \
+    sumcoh_kernel<T, W, R><<<grid_for(n), kThreads, 0, s>>>(D, *props, (const T*)uvw,                  \
+        (const T*)gauss_shape, (const T*)sersic_shape, (const T*)frequency, antenna1, antenna2,        \
+        (const T*)jones, flag, (const T*)weight_vector, (const T*)observed_vis, (const T*)G_term,      \
+        (T*)model_vis, (T*)chi_sqrd_result);                                                           \
+  } while (0)
   if (dtype == MB_FLOAT32) {
     if (w && r) MB_SUMCOH(float, true, true); else if (w) MB_SUMCOH(float, true, false);
     else if (r) MB_SUMCOH(float, false, true); else MB_SUMCOH(float, false, false);
@@ -380,15 +390,20 @@ mb_status mb_reduce_chi2(mb_dtype dtype, const mb_dims* dims, const void* chi_sq
   double* partial = static_cast<double*>(workspace);
   size_t n = size_t(D.ntime) * D.nbl * D.nchan;
   int blocks = int(std::min<size_t>(kReduceBlocks, std::max<size_t>(1, (n + kThreads - 1) / kThreads)));
-  if (dtype == MB_FLOAT32)
+  if (dtype == MB_FLOAT32) {
+    KernelScope ks_("chi2_partial_kernel", s);
     chi2_partial_kernel<float><<<blocks, kThreads, 0, s>>>((const float*)chi_sqrd_result, D.ntime, D.nbl,
         D.nchan, D.lnbl, D.lchan, partial);
-  else if (dtype == MB_FLOAT64)
+  } else if (dtype == MB_FLOAT64) {
+    KernelScope ks_("chi2_partial_kernel", s);
     chi2_partial_kernel<double><<<blocks, kThreads, 0, s>>>((const double*)chi_sqrd_result, D.ntime, D.nbl,
         D.nchan, D.lnbl, D.lchan, partial);
-  else return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
+  } else return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
   MB_CHECK(check_launch("mb_reduce_chi2 partials"));
-  sum_partials_kernel<<<1, 1024, 0, s>>>(partial, blocks, scale, X2_out);
+  {
+    KernelScope ks_("sum_partials_kernel", s);
+    sum_partials_kernel<<<1, 1024, 0, s>>>(partial, blocks, scale, X2_out);
+  }
   return check_launch("mb_reduce_chi2 final");
 }
 

@@ -95,12 +95,18 @@ mb_status mb_tc_selftest(const float* A, const float* B, int K, int mode, float*
     const size_t smem = 4 * StageLayout<MB_MODE_SPLIT_TF32, 128>::kMatBytes;
     MB_CUDA(cudaFuncSetAttribute(tc_selftest_kernel<MB_MODE_SPLIT_TF32>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    tc_selftest_kernel<MB_MODE_SPLIT_TF32><<<1, 160, smem, s>>>(A, B, K, D, status);
+    {
+      KernelScope ks_("tc_selftest_kernel", s);
+      tc_selftest_kernel<MB_MODE_SPLIT_TF32><<<1, 160, smem, s>>>(A, B, K, D, status);
+    }
   } else if (mode == MB_MODE_SPLIT_BF16) {
     const size_t smem = 4 * StageLayout<MB_MODE_SPLIT_BF16, 128>::kMatBytes;
     MB_CUDA(cudaFuncSetAttribute(tc_selftest_kernel<MB_MODE_SPLIT_BF16>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    tc_selftest_kernel<MB_MODE_SPLIT_BF16><<<1, 160, smem, s>>>(A, B, K, D, status);
+    {
+      KernelScope ks_("tc_selftest_kernel", s);
+      tc_selftest_kernel<MB_MODE_SPLIT_BF16><<<1, 160, smem, s>>>(A, B, K, D, status);
+    }
   } else {
     return fail(MB_ERR_INVALID_ARG, "mode must be a split-precision mode");
   }

@@ -41,9 +41,9 @@ WORKLOADS = {
     'small_fp64': dict(ntime=10, na=14, nchan=16, npsrc=20, ngsrc=10, nssrc=0),
     'medium_mixed': dict(ntime=100, na=27, nchan=64, npsrc=1000, ngsrc=200, nssrc=50),
     'large_point': dict(ntime=200, na=64, nchan=256, npsrc=20000, ngsrc=500, nssrc=0),
-    # the large problem's antenna count and sky on a few (time, channel)
-    # units: the case profiled with ncu
-    'profile_point': dict(ntime=4, na=64, nchan=16, npsrc=2000, ngsrc=50, nssrc=0),
+    # the large problem's antennas on fewer times, channels and sources, its
+    # visibility and operand arrays still larger than L2: the ncu case
+    'profile_point': dict(ntime=32, na=64, nchan=64, npsrc=4000, ngsrc=50, nssrc=0),
 }
 
 

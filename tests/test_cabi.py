@@ -12,7 +12,7 @@ HEADER = os.path.join(ROOT, 'include', 'montblanc_gb300.h')
 
 def declared_functions():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r'^\s*(?:const char\*|mb_status|size_t)\s+(mb_\w+)\s*\(', text, re.M)))
+    return sorted(set(re.findall(r'^\s*(?:const char\*|mb_status|size_t|uint64_t)\s+(mb_\w+)\s*\(', text, re.M)))
 
 
 def test_header_declares_entry_points():
@@ -86,3 +86,21 @@ def test_python_error_mapping():
     d = _cabi.make_dims(2, 3, 3, 4, 2)
     with pytest.raises(_cabi.MontblancError, match='MB_ERR_NULL_PTR'):
         _cabi.call('mb_bsqrt', _cabi.MB_FLOAT64, ctypes.byref(d), None, None, None, None, None, None)
+
+
+def test_kernel_timing_without_launches():
+    """Timing switches on and off and reports nothing when nothing launched;
+    rejected calls launch nothing, so the launch counter does not move."""
+    from montblanc_gb300 import _cabi
+    n0 = _cabi.kernel_launches()
+    with _cabi.KernelTimer() as kt:
+        d = _cabi.make_dims(2, 3, 3, 4, 2)
+        _cabi.lib.mb_bsqrt(_cabi.MB_FLOAT64, ctypes.byref(d), None, None, None, None, None, None)
+    assert kt.launches == 0
+    assert kt.times() == {}
+    assert _cabi.kernel_launches() == n0
+    ms, n = ctypes.c_double(-1.0), ctypes.c_int64(-1)
+    _cabi.call('mb_kernel_time', None, ctypes.byref(ms), ctypes.byref(n))
+    assert (ms.value, n.value) == (0.0, 0)
+    st = _cabi.lib.mb_kernel_time(None, None, ctypes.byref(n))
+    assert _cabi.STATUS_NAMES[st] == 'MB_ERR_NULL_PTR'

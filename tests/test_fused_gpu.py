@@ -92,3 +92,19 @@ def test_fused_non_default_antenna_pairs():
     assert golden_io.rel_err(vis.cpu().numpy(), out) < 1e-10
     assert golden_io.rel_err(chi2.cpu().numpy(), terms) < 1e-10
     assert abs(x2 - X2) <= 1e-10 * abs(X2)
+
+
+def test_kernel_timer_reports_the_fused_launches():
+    """Per-kernel event timing sees the fused kernels of one forward."""
+    from montblanc_gb300 import _cabi
+    from montblanc_gb300.rime import RimeProblem
+    P, ref = golden_io.load('small_fp64')
+    prob = RimeProblem.from_numpy(P, dtype='float')
+    prob.forward()
+    with _cabi.KernelTimer() as kt:
+        x2 = prob.forward().item()
+    times = kt.times()
+    assert 'coh_fwd_kernel' in times and 'sum_partials_kernel' in times
+    assert kt.launches == sum(n for _, n in times.values())
+    assert all(ms >= 0.0 for ms, _ in times.values())
+    assert abs(x2 - ref['X2']) <= TOL['float']['X2'] * abs(ref['X2'])
