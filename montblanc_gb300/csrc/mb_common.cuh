@@ -162,6 +162,10 @@ template <> __device__ __forceinline__ void jstore<double>(double* p, const Jone
 
 // ---- scalar helpers -------------------------------------------------------
 __device__ __forceinline__ float mb_sqrt(float x) { return sqrtf(x); }
+// 1 / sqrt(x): the hardware reciprocal square root in FP32 (a few ulp), the
+// correctly rounded quotient in FP64.  +inf for x == 0 in both.
+__device__ __forceinline__ float mb_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double mb_rsqrt(double x) { return 1.0 / sqrt(x); }
 __device__ __forceinline__ double mb_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float mb_exp(float x) { return expf(x); }
 __device__ __forceinline__ double mb_exp(double x) { return exp(x); }
@@ -302,8 +306,7 @@ __device__ __forceinline__ void beam_corner(const T* __restrict__ E_beam, const 
 
 template <typename T>
 __device__ __forceinline__ Cx<T> renorm(Cx<T> z, T amp) {
-  T r = cabs_(z);
-  T norm = T(1) / r;
+  T norm = mb_rsqrt(z.r * z.r + z.i * z.i);
   if (!isfinite(norm)) norm = T(1);
   return z * (norm * amp);
 }
@@ -399,6 +402,10 @@ __device__ __forceinline__ T sersic_shape(T u, T v, T e1, T e2, T R, T k) {
   T u1 = (u * (T(1) + e1) + v * e2) * k * S;
   T v1 = (u * e2 + v * (T(1) - e1)) * k * S;
   T d = T(1) + u1 * u1 + v1 * v1;
+  if constexpr (sizeof(T) == 4) {
+    const T r = mb_rsqrt(d);
+    return r * r * r;
+  }
   return T(1) / (d * mb_sqrt(d));
 }
 

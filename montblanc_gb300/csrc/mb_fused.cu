@@ -39,7 +39,9 @@ template <> struct FwdTile<float> { static constexpr int RP = 2, RQ = 4, ST = 16
 template <> struct FwdTile<double> { static constexpr int RP = 1, RQ = 2, ST = 8; };
 template <typename T> struct AdjTile;
 // FULL_Y: the Hermitian matrix Y of d chi^2 / dV is kept complete (na x na
-// Jones) in shared memory; otherwise only its packed upper triangle.
+// Jones) in shared memory; otherwise only its packed upper triangle.  Full
+// rows are padded by 16 bytes (y_row_vals), so that lanes reading the same
+// column of consecutive rows hit distinct banks.
 template <> struct AdjTile<float> {
   static constexpr int RA = 2, RS = 4, ST = 16, THREADS = 512;
   static constexpr bool FULL_Y = true;
@@ -50,7 +52,16 @@ template <> struct AdjTile<double> {
 };
 
 constexpr int kNAcc = 10;  // l, m, I, Q, U, V, alpha, shape0, shape1, shape2
-constexpr int kBsqVals = 8;  // values per (source, time) entry of the sqrt(B) table
+
+// Values (T) per row of the full Y in shared memory: na Jones + 16 bytes.
+template <typename T>
+__host__ __device__ __forceinline__ int y_row_vals(int na) { return 8 * na + int(16 / sizeof(T)); }
+
+template <typename T>
+__device__ __forceinline__ T* y_full(T* sY, int a, int b, int na) { return sY + a * y_row_vals<T>(na) + 8 * b; }
+// Values per (source, time) entry of the sqrt(B) table: sqrt(B) at nu_ref
+// (a, d, Re b, Im b), alpha / 2, 0, l / n, m / n.
+constexpr int kBsqVals = 8;
 
 int count_pair_tiles(int na, int RP, int RQ) {
   int npt = (na + RP - 1) / RP, nqt = (na + RQ - 1) / RQ, n = 0;
@@ -58,8 +69,9 @@ int count_pair_tiles(int na, int RP, int RQ) {
   return n;
 }
 
+// with_J = false leaves out the Jones tile (a caller that places it itself).
 template <typename T>
-SmemPlan make_plan(int na, bool adjoint) {
+SmemPlan make_plan(int na, bool adjoint, bool with_J = true) {
   SmemPlan S;
   S.nap = (na + 3) / 4 * 4;
   S.st = adjoint ? AdjTile<T>::ST : FwdTile<T>::ST;
@@ -81,9 +93,10 @@ SmemPlan make_plan(int na, bool adjoint) {
   S.off_ant = take(sizeof(AntInfo<T>) * na);
   S.off_antd = take(0);
   S.off_src = take(sizeof(SrcInfo<T>) * S.st);
-  S.off_J = take(sizeof(Jones<T>) * S.st * S.nap);
+  S.off_J = take(with_J ? sizeof(Jones<T>) * S.st * S.nap : 0);
   S.off_gJ = take(adjoint ? sizeof(Jones<T>) * S.st * S.nap : 0);
-  S.off_V = take(sizeof(Jones<T>) * (adjoint && AdjTile<T>::FULL_Y ? size_t(na) * na : size_t(S.npairs)));
+  S.off_V = take(adjoint && AdjTile<T>::FULL_Y ? sizeof(T) * size_t(na) * y_row_vals<T>(na)
+                                                : sizeof(Jones<T>) * size_t(S.npairs));
   // FP32 forward: low parts of float-float pair accumulators
   S.off_Vlo = take(!adjoint && sizeof(T) == 4 ? sizeof(Jones<T>) * S.npairs : 0);
   S.off_items = take(adjoint ? 0 : sizeof(int) * (S.nitems + 128));
@@ -447,9 +460,12 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A,
 // Per (time, channel) unit, with A (128 x 4k) the per-stage operand whose row
 // r = 2a + i holds, for the stage's k sources s and Jones columns c,
 // Re J_s,a[i][c] (K index 2s + c) and Im J_s,a[i][c] (K index 2k + 2s + c):
-//   D_re = A A^T            = Re sum_s J_a J_b^H  (rows 2a+i, columns 2b+j)
-//   D_x  = A_im A_re^T,  Im sum_s J_a J_b^H = D_x - D_x^T,
-// with each operand value split into hi + lo parts: the large hi.hi products
+//   D_re = A A^T                      = Re sum_s J_a J_b^H  (rows 2a+i, columns 2b+j)
+//   D_im = A_im A_re^T - A_re A_im^T  = Im sum_s J_a J_b^H
+// (the second product with the instruction's negate-A bit).  D_re is
+// symmetric and D_im antisymmetric, so each antenna pair is drained once,
+// from whichever of (a, b), (b, a) the cyclic rule in tc_drain picks.
+// Each operand value is split into hi + lo parts: the large hi.hi products
 // and the small hi.lo + lo.hi corrections accumulate in separate TMEM
 // accumulators (FP32), which are folded into float-float pair accumulators
 // in shared memory every kTcGroup stages.  The tensor core's FP32
@@ -459,10 +475,10 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A,
 // sources near 1e-7 relative.
 constexpr int kTcProducers = 256;          // warps 0-7: operands, TMEM drain
 constexpr int kTcThreads = kTcProducers + 32;  // warp 8: MMA issue
-constexpr int kTcStages = 3;
-constexpr int kTcRowBytes = 64;  // 4 sources (TF32) / 8 sources (BF16) per stage
-constexpr int kTcGroup = 16;               // stages per TMEM accumulation group
-// TMEM columns: D_re 0-127, D_x 128-255 (hi.hi); their corrections 256-511.
+constexpr int kTcStages = 2;
+constexpr int kTcRowBytes = 128;  // 8 sources (TF32) / 16 sources (BF16) per stage
+constexpr int kTcGroup = 8;                // stages per TMEM accumulation group
+// TMEM columns: D_re 0-127, D_im 128-255 (hi.hi); their corrections 256-511.
 constexpr uint32_t kTcCols = 512;
 
 struct TcPlan {
@@ -496,34 +512,49 @@ __device__ __forceinline__ void fold_scalar(float* hi, float* lo, float x) {
   *lo += err;
 }
 
-// Drain TMEM into the float-float pair accumulators (producer threads).
+// Whether row antenna a drains its block with column antenna b: each
+// unordered pair once, from the row whose cyclic distance to the other is
+// below na / 2 (ties: the smaller index), so every row drains about na / 2
+// columns and the producer warps share the drain evenly.
+__device__ __forceinline__ bool tc_drains(int a, int b, int na) {
+  int d = b - a;
+  if (d < 0) d += na;
+  return 2 * d < na || (2 * d == na && a < b);
+}
+
+// Drain TMEM into the float-float pair accumulators (producer threads):
+// warps 0-3 D_re, warps 4-7 D_im, each its 32 TMEM lanes (rows 2a + i).
 __device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, float* sVlof) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int q = warp & 3, h = warp >> 2;
   const int r = 32 * q + lane, a = r >> 1, i = r & 1;
-  const bool row_ok = a < A.na;
+  const int na = A.na;
+  const bool row_ok = a < na;
+  const int dmax = (na - 1) / 2 + ((na % 2 == 0 && a < na / 2) ? 1 : 0);  // drained b: a .. a + dmax (cyclic)
   const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(h * 128);
-  for (int pass = 0; pass < 2; ++pass) {
-    if (pass == 1) named_sync_producers();
-    if (pass == 1 && h == 0) continue;
-    for (int c0 = 0; c0 < 128; c0 += 32) {
-      float v[32], w[32];
-      tc::tmem_ld32(lane_addr + c0, v);
-      tc::tmem_ld32(lane_addr + 256 + c0, w);
+  for (int c0 = 0; c0 < 128; c0 += 32) {
+    const int b_lo = c0 >> 1, b_hi = min(b_lo + 15, na - 1);
+    // does the cyclic interval [a, a + dmax] meet [b_lo, b_hi]?  (warp-uniform skip)
+    int x = b_lo - a, y = a - b_lo;
+    if (x < 0) x += na;
+    if (y < 0) y += na;
+    const bool meets = row_ok && b_lo < na && (x <= dmax || y <= b_hi - b_lo);
+    if (!__any_sync(0xffffffffu, meets)) continue;
+    float v[32], w[32];
+    tc::tmem_ld32(lane_addr + c0, v);
+    tc::tmem_ld32(lane_addr + 256 + c0, w);
+    if (!meets) continue;
 #pragma unroll
-      for (int c = 0; c < 32; ++c) v[c] += w[c];
-      if (!row_ok) continue;
-#pragma unroll
-      for (int c = 0; c < 32; ++c) {
-        const int n = c0 + c, b = n >> 1, j = n & 1;
-        if (b >= A.na) continue;
-        if (pass == 0 && b >= a) {
-          const int e = pair_index(a, b, A.na) * 8 + (2 * i + j) * 2 + h;  // h=0: re, h=1: im
-          fold_scalar(sVf + e, sVlof + e, v[c]);
-        } else if (pass == 1 && b <= a) {
-          const int e = pair_index(b, a, A.na) * 8 + (2 * j + i) * 2 + 1;
-          fold_scalar(sVf + e, sVlof + e, -v[c]);
-        }
+    for (int c = 0; c < 32; ++c) {
+      const int n = c0 + c, b = n >> 1, j = n & 1;
+      if (b >= na || !tc_drains(a, b, na)) continue;
+      const float val = v[c] + w[c];
+      if (a <= b) {
+        const int e = pair_index(a, b, na) * 8 + (2 * i + j) * 2 + h;  // h = 0: re, 1: im
+        fold_scalar(sVf + e, sVlof + e, val);
+      } else {  // V_ba = (sum J_a J_b^H)^H: transpose, conjugate
+        const int e = pair_index(b, a, na) * 8 + (2 * j + i) * 2 + h;
+        fold_scalar(sVf + e, sVlof + e, h ? -val : val);
       }
     }
   }
@@ -550,6 +581,34 @@ __device__ __forceinline__ SrcInfo<float> point_source_info(const FusedArgs<floa
   const float* S = A.stokes + 4 * st;
   const float power = mb_pow(__ldg(A.freq + ch) / __ldg(A.ref_freq + ch), __ldg(A.alpha + st));
   si.B = brightness_sqrt<float>(__ldg(S), __ldg(S + 1), __ldg(S + 2), __ldg(S + 3), power);
+  return si;
+}
+
+// Source terms for the point-source chain at (time t, channel ch): those of
+// point_source_info plus l / n and m / n from the sqrt(B) table.
+__device__ __forceinline__ SrcInfo<float> point_source_chain_info(const FusedArgs<float>& A, int t, int ch, int s,
+                                                                 float log2_ratio) {
+  SrcInfo<float> si = point_source_info(A, t, ch, s, log2_ratio);
+  if (A.bsq0) {
+    const float2 q = __ldg(reinterpret_cast<const float2*>(A.bsq0 + kBsqVals * (size_t(s) * A.ntime + t) + 6));
+    si.l_over_n = q.x;
+    si.m_over_n = q.y;
+  } else {
+    const double l = si.l, m = si.m, n = sqrt(1.0 - l * l - m * m);
+    si.l_over_n = float(l / n);
+    si.m_over_n = float(m / n);
+  }
+  return si;
+}
+
+// Stokes parameters, power and sqrt(B) of point source s at (t, ch), FP32.
+__device__ __forceinline__ SrcInfo<float> point_source_stokes(const FusedArgs<float>& A, int t, int ch, int s,
+                                                             float log2_ratio) {
+  SrcInfo<float> si = point_source_info(A, t, ch, s, log2_ratio);
+  const size_t st = size_t(s) * A.ltime + t;
+  const float* S = A.stokes + 4 * st;
+  si.I = S[0]; si.Q = S[1]; si.U = S[2]; si.V = S[3];
+  si.power = mb_pow(__ldg(A.freq + ch) / __ldg(A.ref_freq + ch), __ldg(A.alpha + st));
   return si;
 }
 
@@ -669,6 +728,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   } else if (lane == 0) {
     // ---- MMA issue ---------------------------------------------------------
     const uint32_t idesc = L::instr(128, 128);
+    const uint32_t idesc_neg = idesc | (1u << 13);  // negate A
     const int half = L::kKSteps / 2;
     bool issued = false;
     for (int g = 0; g < nstages && !*abort_flag; ++g) {
@@ -698,9 +758,14 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
         const uint64_t ih = L::desc(hi + oi), il = L::desc(lo + oi);
         const uint64_t rh = L::desc(hi + orr), rl = L::desc(lo + orr);
         const uint32_t acc = kk == 0 ? acc0 : 1u;
+        // D_im += A_im A_re^T
         L::mma(tmem + 128, ih, rh, idesc, acc);
         L::mma(tmem + 384, ih, rl, idesc, acc);
         L::mma(tmem + 384, il, rh, idesc, 1u);
+        // D_im += (-A_re) A_im^T
+        L::mma(tmem + 128, rh, ih, idesc_neg, 1u);
+        L::mma(tmem + 384, rh, il, idesc_neg, 1u);
+        L::mma(tmem + 384, rl, ih, idesc_neg, 1u);
       }
       issued = true;
       tc::mma_commit(empty + slot);
@@ -753,7 +818,7 @@ __device__ __forceinline__ Jones<T> y_entry(const Jones<T>* sX, int a, int b, in
 
 template <typename T>
 __device__ __forceinline__ Jones<T> y_at(const Jones<T>* sY, int a, int b, int na) {
-  if (AdjTile<T>::FULL_Y) return sY[a * na + b];
+  if (AdjTile<T>::FULL_Y) return jload<T>(y_full(reinterpret_cast<const T*>(sY), a, b, na));
   return y_entry(sY, a, b, na);
 }
 
@@ -784,7 +849,7 @@ __device__ void adj_consume_point_full(const FusedArgs<T>& A, const SmemPlan& S,
         Jones<T> Y[TA], J[TS];
 #pragma unroll
         for (int r = 0; r < TA; ++r)
-          Y[r] = (a0 + r < A.na) ? jload<T>(reinterpret_cast<const T*>(sY + (a0 + r) * A.na + b)) : jzero<T>();
+          Y[r] = (a0 + r < A.na) ? jload<T>(y_full(reinterpret_cast<const T*>(sY), a0 + r, b, A.na)) : jzero<T>();
 #pragma unroll
         for (int c = 0; c < TS; ++c) {
           const int si = min(sb + c, ns - 1);
@@ -849,8 +914,7 @@ __device__ void beam_interp_d(const T* __restrict__ E_beam, const BeamGeom& G, c
   const Cx<T>* s4 = &sum.a; const Cx<T>* l4 = &dsl.a; const Cx<T>* m4 = &dsm.a;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    T r = cabs_(s4[k]);
-    T inv = T(1) / r;
+    T inv = mb_rsqrt(s4[k].r * s4[k].r + s4[k].i * s4[k].i);
     if (isfinite(inv)) {
       E4[k] = s4[k] * (amp[k] * inv);
       T drl = cdot_re(s4[k], l4[k]) * inv, drm = cdot_re(s4[k], m4[k]) * inv;
@@ -893,8 +957,7 @@ __device__ void beam_interp_plane_d(const T* __restrict__ plane, int mh, const G
   const Cx<T>* s4 = &sum.a; const Cx<T>* l4 = &dsl.a; const Cx<T>* m4 = &dsm.a;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    T r = cabs_(s4[k]);
-    T inv = T(1) / r;
+    T inv = mb_rsqrt(s4[k].r * s4[k].r + s4[k].i * s4[k].i);
     if (isfinite(inv)) {
       E4[k] = s4[k] * (amp[k] * inv);
       T drl = cdot_re(s4[k], l4[k]) * inv, drm = cdot_re(s4[k], m4[k]) * inv;
@@ -927,7 +990,13 @@ __device__ __forceinline__ T shape_and_grad(int type, T u, T v, T p0, T p1, T p2
   T a1 = u * (T(1) + e1) + v * e2, b1 = u * e2 + v * (T(1) - e1);
   T u1 = a1 * ks * Sc, v1 = b1 * ks * Sc;
   T dd = T(1) + u1 * u1 + v1 * v1;
-  T c = T(1) / (dd * mb_sqrt(dd));
+  T c;
+  if constexpr (sizeof(T) == 4) {
+    const T r = mb_rsqrt(dd);
+    c = r * r * r;
+  } else {
+    c = T(1) / (dd * mb_sqrt(dd));
+  }
   T dS1 = Sc * T(2) * e1 / den, dS2 = Sc * T(2) * e2 / den;
   T du_e1 = ks * (u * Sc + a1 * dS1), dv_e1 = ks * (-v * Sc + b1 * dS1);
   T du_e2 = ks * (v * Sc + a1 * dS2), dv_e2 = ks * (u * Sc + b1 * dS2);
@@ -973,41 +1042,72 @@ __device__ void adj_consume_point(const FusedArgs<T>& A, const SmemPlan& S, int 
   }
 }
 
+// Adds the NV values of every active lane to acc[key * kNAcc + first + j].
+// When all active lanes of the warp share one key the warp sums first and
+// one lane adds; otherwise each active lane adds its own.  Every lane of the
+// warp calls it; key < 0 marks an inactive lane (its values must be 0).
+template <typename T, int NV>
+__device__ __forceinline__ void warp_keyed_add(T* acc, int first, int key, T (&v)[NV]) {
+  const unsigned full = 0xffffffffu;
+  const int k0 = __reduce_max_sync(full, key);
+  if (__all_sync(full, key < 0 || key == k0)) {
+    if (k0 < 0) return;
+#pragma unroll
+    for (int j = 0; j < NV; ++j)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(full, v[j], o);
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+      for (int j = 0; j < NV; ++j) atomicAdd(acc + k0 * kNAcc + first + j, v[j]);
+  } else if (key >= 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) atomicAdd(acc + key * kNAcc + first + j, v[j]);
+  }
+}
+
+// dJ_a(s) = sum_b shape_s(a, b) Y_ab J_b(s) for the extended sources of a
+// tile, with d chi^2 / d(shape parameters) from the pairs a < b.  Work item
+// (source, antenna a); the lanes of a warp take consecutive antennas.
 template <typename T>
 __device__ void adj_consume_ext(const FusedArgs<T>& A, const SmemPlan& S, int ns, const SrcInfo<T>* ss,
                                 const AntInfo<T>* sa, const Jones<T>* sJ, const Jones<T>* sX, Jones<T>* sgJ,
                                 T* sacc, T kg, T ks) {
-  for (int k = threadIdx.x; k < ns * A.na; k += blockDim.x) {
-    const int si = k / A.na, a = k - si * A.na;
-    const SrcInfo<T>& src = ss[si];
-    const Jones<T> Ja = sJ[si * S.nap + a];
-    Jones<T> acc = jzero<T>();
-    T g0 = 0, g1 = 0, g2 = 0;
-    for (int b = 0; b < A.na; ++b) {
-      Jones<T> Y = y_at(sX, a, b, A.na);
-      Jones<T> P = jmul(Y, sJ[si * S.nap + b]);
-      T d[3];
-      T c = shape_and_grad<T>(src.type, sa[b].u - sa[a].u, sa[b].v - sa[a].v, src.s0, src.s1, src.s2, kg, ks, d);
-      acc = jadd(acc, jscale(P, c));
-      if (a < b) {
-        T gc = jdot_re(Ja, P);
-        g0 += gc * d[0]; g1 += gc * d[1]; g2 += gc * d[2];
+  const int n = ns * A.na;
+  const int rounds = (n + blockDim.x - 1) / blockDim.x;
+  for (int round = 0; round < rounds; ++round) {
+    const int k = round * blockDim.x + threadIdx.x;
+    const bool active = k < n;
+    const int si = active ? k / A.na : 0, a = active ? k - si * A.na : 0;
+    T g[3] = {T(0), T(0), T(0)};
+    if (active) {
+      const SrcInfo<T>& src = ss[si];
+      const Jones<T>* Js = sJ + si * S.nap;
+      const Jones<T> Ja = Js[a];
+      const T ua = sa[a].u, va = sa[a].v;
+      Jones<T> acc = jzero<T>();
+      for (int b = 0; b < A.na; ++b) {
+        const Jones<T> P = jmul(y_at(sX, a, b, A.na), Js[b]);
+        T d[3];
+        const T c = shape_and_grad<T>(src.type, sa[b].u - ua, sa[b].v - va, src.s0, src.s1, src.s2, kg, ks, d);
+        acc = jadd(acc, jscale(P, c));
+        if (a < b) {
+          const T gc = jdot_re(Ja, P);
+          g[0] += gc * d[0]; g[1] += gc * d[1]; g[2] += gc * d[2];
+        }
       }
+      sgJ[si * S.nap + a] = acc;
     }
-    sgJ[si * S.nap + a] = acc;
-    atomicAdd(&sacc[si * kNAcc + 7], g0);
-    atomicAdd(&sacc[si * kNAcc + 8], g1);
-    atomicAdd(&sacc[si * kNAcc + 9], g2);
+    warp_keyed_add<T, 3>(sacc, 7, active ? si : -1, g);
   }
 }
 
-// Chain d chi^2 / dJ(s, a) through E, K and sqrt(B): the contributions to
-// d chi^2 / d(l, m, I, Q, U, V, alpha) of source s.
+// Chain d chi^2 / dJ(s, a) through E and K: d chi^2 / d(l, m) of the item
+// and gB = d chi^2 / d sqrt(B) (complex, per Jones entry).  Uses src.l, m,
+// l_over_n, m_over_n and B.
 template <typename T>
-__device__ __forceinline__ void chain_item(const FusedArgs<T>& A, int t, int ch, int s, int a, const SrcInfo<T>& src,
+__device__ __forceinline__ void chain_core(const FusedArgs<T>& A, int t, int ch, int s, int a, const SrcInfo<T>& src,
                                            const AntInfo<T>& ai, const Jones<T>& gJ, T f, double nu_over_c,
-                                           T half_log_ratio, const ChanPos<T>& cp, T (&g)[7]) {
-  const double dphase = 2.0 * kPi * nu_over_c;  // |dK/dphi|
+                                           T dphase, const ChanPos<T>& cp, T& gl0, T& gm0, Jones<T>& gB) {
   const BeamGeom G{A.lw, A.mh, A.nud};
   Cx<T> K = phase_term(A, t, s, a, f, nu_over_c);
   T l, m;
@@ -1025,17 +1125,25 @@ __device__ __forceinline__ void chain_item(const FusedArgs<T>& A, int t, int ch,
   Jones<T> gE = jmulh(gJ, KB);
   T g_ld = gl.inside ? jdot_re(gE, dEl) * A.lscale : T(0);
   T g_md = gm.inside ? jdot_re(gE, dEm) * A.mscale : T(0);
-  T gl0 = g_ld * ai.sc_l * ai.cos_pa + g_md * ai.sc_m * ai.sin_pa;
-  T gm0 = -g_ld * ai.sc_l * ai.sin_pa + g_md * ai.sc_m * ai.cos_pa;
+  gl0 = g_ld * ai.sc_l * ai.cos_pa + g_md * ai.sc_m * ai.sin_pa;
+  gm0 = -g_ld * ai.sc_l * ai.sin_pa + g_md * ai.sc_m * ai.cos_pa;
   // K and sqrt(B)
   Jones<T> gKB = jhmul(E, gJ);
   Cx<T> gK = cmulc(gKB.a, B.a) + cmulc(gKB.b, B.b) + cmulc(gKB.c, B.c) + cmulc(gKB.d, B.d);
-  T gphi = T(dphase) * (gK.r * K.i - gK.i * K.r);
+  T gphi = dphase * (gK.r * K.i - gK.i * K.r);
   gl0 += gphi * (ai.u - ai.w * src.l_over_n);
   gm0 += gphi * (ai.v - ai.w * src.m_over_n);
   Cx<T> Kc = conj(K);
-  Jones<T> gB = {cmul(Kc, gKB.a), cmul(Kc, gKB.b), cmul(Kc, gKB.c), cmul(Kc, gKB.d)};
-  T GB = jdot_re(gB, B);
+  gB = {cmul(Kc, gKB.a), cmul(Kc, gKB.b), cmul(Kc, gKB.c), cmul(Kc, gKB.d)};
+}
+
+// d chi^2 / d(I, Q, U, V, alpha) of a source from gB = d chi^2 / d sqrt(B)
+// at its (time, channel).  Linear in gB, so gB may be a sum over antennas.
+// Uses src.B, I, Q, U, V and power.
+template <typename T>
+__device__ __forceinline__ void stokes_grads(const SrcInfo<T>& src, const Jones<T>& gB, T half_log_ratio,
+                                             T (&g)[5]) {
+  const T GB = jdot_re(gB, src.B);
   const T det0 = src.I * src.I - src.Q * src.Q - src.U * src.U - src.V * src.V;
   const T s0v = mb_sqrt(det0 > T(0) ? det0 : T(0));
   T gI = 0, gQ = 0, gU = 0, gVv = 0;
@@ -1049,8 +1157,23 @@ __device__ __forceinline__ void chain_item(const FusedArgs<T>& A, int t, int ch,
     gU = pt * ((gB.b.r + gB.c.r) - (src.U / s0v) * tr1) + q2 * src.U;
     gVv = pt * ((gB.b.i - gB.c.i) - (src.V / s0v) * tr1) + q2 * src.V;
   }
-  g[0] = gl0; g[1] = gm0; g[2] = gI; g[3] = gQ; g[4] = gU; g[5] = gVv;
-  g[6] = GB * half_log_ratio;
+  g[0] = gI; g[1] = gQ; g[2] = gU; g[3] = gVv;
+  g[4] = GB * half_log_ratio;
+}
+
+// Chain d chi^2 / dJ(s, a) through E, K and sqrt(B): the contributions to
+// d chi^2 / d(l, m, I, Q, U, V, alpha) of source s.
+template <typename T>
+__device__ __forceinline__ void chain_item(const FusedArgs<T>& A, int t, int ch, int s, int a, const SrcInfo<T>& src,
+                                           const AntInfo<T>& ai, const Jones<T>& gJ, T f, double nu_over_c,
+                                           T half_log_ratio, const ChanPos<T>& cp, T (&g)[7]) {
+  const T dphase = T(2.0 * kPi * nu_over_c);  // |dK/dphi|
+  Jones<T> gB;
+  chain_core(A, t, ch, s, a, src, ai, gJ, f, nu_over_c, dphase, cp, g[0], g[1], gB);
+  T gs[5];
+  stokes_grads(src, gB, half_log_ratio, gs);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) g[2 + k] = gs[k];
 }
 
 // Chain d chi^2 / dJ through E, K and sqrt(B) to the source parameters.
@@ -1061,13 +1184,16 @@ __device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int c
   const T f = A.freq[ch];
   const double nu_over_c = double(f) / kLightSpeed;
   const T half_log_ratio = T(0.5) * mb_log(f / A.ref_freq[ch]);
-  for (int i = threadIdx.x; i < ns * A.na; i += blockDim.x) {
-    const int si = i / A.na, a = i - si * A.na;
-    T g[7];
-    chain_item(A, t, ch, s0 + si, a, ss[si], sa[a], sgJ[si * S.nap + a], f, nu_over_c, half_log_ratio, cp, g);
-    T* acc = sacc + si * kNAcc;
-#pragma unroll
-    for (int k = 0; k < 7; ++k) atomicAdd(acc + k, g[k]);
+  const int n = ns * A.na;
+  const int rounds = (n + blockDim.x - 1) / blockDim.x;
+  for (int round = 0; round < rounds; ++round) {
+    const int i = round * blockDim.x + threadIdx.x;
+    const bool active = i < n;
+    const int si = active ? i / A.na : 0, a = active ? i - si * A.na : 0;
+    T g[7] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+    if (active)
+      chain_item(A, t, ch, s0 + si, a, ss[si], sa[a], sgJ[si * S.nap + a], f, nu_over_c, half_log_ratio, cp, g);
+    warp_keyed_add<T, 7>(sacc, 0, active ? si : -1, g);
   }
 }
 
@@ -1102,8 +1228,8 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
   const int unit = blockIdx.x;
   const int t = unit / A.nchan, ch = unit - t * A.nchan;
   load_antennas(A, t, ch, sa);
-  const int nx = AdjTile<T>::FULL_Y ? A.na * A.na : S.npairs;
-  for (int i = threadIdx.x; i < nx; i += blockDim.x) sX[i] = jzero<T>();
+  const int nx = AdjTile<T>::FULL_Y ? A.na * y_row_vals<T>(A.na) : 8 * S.npairs;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) reinterpret_cast<T*>(sX)[i] = T(0);
   for (int i = threadIdx.x; i < S.st * kNAcc; i += blockDim.x) sacc[i] = T(0);
   __syncthreads();
   for (int bl = threadIdx.x; bl < A.nbl; bl += blockDim.x) {
@@ -1113,8 +1239,8 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
     Jones<T> g = jload<T>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch));
     if (AdjTile<T>::FULL_Y) {
       // baseline (p, q): Y_pq += gV, Y_qp += gV^H (p == q: both terms)
-      atomic_add_jones(&sX[p * A.na + q], g);
-      atomic_add_jones(&sX[q * A.na + p], jherm(g));
+      atomic_add_jones(reinterpret_cast<Jones<T>*>(y_full(reinterpret_cast<T*>(sX), p, q, A.na)), g);
+      atomic_add_jones(reinterpret_cast<Jones<T>*>(y_full(reinterpret_cast<T*>(sX), q, p, A.na)), jherm(g));
     } else if (p <= q) {
       atomic_add_jones(&sX[pair_index(p, q, A.na)], g);
     } else {
@@ -1167,6 +1293,7 @@ constexpr int kTaProducers = 128;     // warps 0-3
 constexpr int kTaChain = 256;         // warps 4-11
 constexpr int kTaThreads = kTaProducers + kTaChain + 32;  // warp 12: MMA
 constexpr uint32_t kTaCols = 64;      // 2 buffers x (D_re 16 + D_im 16)
+constexpr int kTaAcc = 10;            // per-source sums: d/dl, d/dm, gB (8)
 using TaGeom = StageGeometry<kTaRowBytes>;
 using TaLayout = StageLayout<MB_MODE_SPLIT_BF16, kTaRowBytes>;
 constexpr size_t kYopBytes = 2 * size_t(TaGeom::kMatBytes);          // hi + lo: 128 KB
@@ -1241,7 +1368,7 @@ __global__ void __launch_bounds__(kTaThreads) coh_tc_adj_kernel(FusedArgs<float>
   unsigned char* syop = smem + P.off_yop;
   unsigned char* stage = smem + P.off_stage;
   AntInfo<float>* sa = reinterpret_cast<AntInfo<float>*>(smem + P.off_ant);
-  float* sacc = reinterpret_cast<float*>(smem + P.off_acc);  // [kTaKappa][7]
+  float* sacc = reinterpret_cast<float*>(smem + P.off_acc);  // [kTaKappa][kTaAcc]
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + P.off_bar);
   uint64_t* full = bars;                    // [kTaStages]
   uint64_t* empty = bars + kTaStages;       // [kTaStages]
@@ -1266,7 +1393,7 @@ __global__ void __launch_bounds__(kTaThreads) coh_tc_adj_kernel(FusedArgs<float>
     for (int i = tid; i < int(kYopBytes / 16); i += blockDim.x) dst[i] = __ldg(src + i);
   }
   load_antennas(A, t, ch, sa);
-  for (int i = tid; i < kTaKappa * 7; i += blockDim.x) sacc[i] = 0.f;
+  for (int i = tid; i < kTaKappa * kTaAcc; i += blockDim.x) sacc[i] = 0.f;
   if (tid == 0) {
     for (int i = 0; i < kTaStages; ++i) {
       tc::mbar_init(full + i, kTaProducers);
@@ -1290,7 +1417,13 @@ __global__ void __launch_bounds__(kTaThreads) coh_tc_adj_kernel(FusedArgs<float>
   const ChanPos<float> cp = chan_pos<float>(f, A.lfreq, A.ufreq, A.nud);
   const float log2_ratio = log2f(f / A.ref_freq[ch]);
   const float half_log_ratio = 0.5f * logf(f / A.ref_freq[ch]);
+  const float dphase = float(2.0 * kPi * nu_over_c);
   const int ntiles = (A.npsrc + kTaKappa - 1) / kTaKappa;
+  // Units start their tile sweep at different tiles, so that the CTAs in
+  // flight (neighbouring channels) do not update the same sources' FP64
+  // accumulators at the same time.
+  const int rot = int((unsigned(unit) * 2654435761u) % unsigned(max(ntiles, 1)));
+  auto tile_of = [&](int g) { const int x = g + rot; return x >= ntiles ? x - ntiles : x; };
 
   if (warp < 4) {
     // ---- producers: J of the tile's (source, antenna) pairs into Jop ------
@@ -1298,7 +1431,7 @@ __global__ void __launch_bounds__(kTaThreads) coh_tc_adj_kernel(FusedArgs<float>
     for (int g = 0; g < ntiles && !bad; ++g) {
       const int slot = g % kTaStages, use = g / kTaStages;
       if (!tc::mbar_wait(empty + slot, (use & 1) ^ 1)) { bad = true; break; }
-      const int s0 = g * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
+      const int s0 = tile_of(g) * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
       unsigned char* hi = stage + size_t(slot) * kJopBytes;
       unsigned char* lo = hi + kJopBytes / 2;
 #pragma unroll 1
@@ -1334,60 +1467,89 @@ __global__ void __launch_bounds__(kTaThreads) coh_tc_adj_kernel(FusedArgs<float>
       tc::tmem_ld32(tmem + (uint32_t(32 * q) << 16) + uint32_t(32 * buf), v);
       tc::fence_before_thread_sync();
       tc::mbar_arrive(dfree + buf);
-      // own row i of dJ for the set's 4 sources; the partner lane holds row 1-i
-      // give the partner the sources it chains: lane i=0 chains base+0,1,
-      // lane i=1 chains base+2,3
+      // The set's 4 sources (warp-uniform choice, constant indices):
+      // w[2j + k] = Re dJ(base + j)[i][k], w[8 + 2j + k] = Im dJ(base + j)[i][k].
+      float w[16];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        w[e] = set ? v[8 + e] : v[e];
+        w[8 + e] = set ? v[24 + e] : v[16 + e];
+      }
+      // own row i of dJ; the partner lane holds row 1 - i.  Lane i = 0
+      // chains sources j = 0, 1 of the set, lane i = 1 sources j = 2, 3: each
+      // gives the partner its row of the partner's sources.
       float give[8], recv[8];
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
-        const int sl = base + (i ? u : 2 + u);
-        give[4 * u + 0] = v[2 * sl];      give[4 * u + 1] = v[2 * sl + 1];
-        give[4 * u + 2] = v[16 + 2 * sl]; give[4 * u + 3] = v[16 + 2 * sl + 1];
+        give[4 * u + 0] = i ? w[2 * u] : w[2 * (2 + u)];
+        give[4 * u + 1] = i ? w[2 * u + 1] : w[2 * (2 + u) + 1];
+        give[4 * u + 2] = i ? w[8 + 2 * u] : w[8 + 2 * (2 + u)];
+        give[4 * u + 3] = i ? w[8 + 2 * u + 1] : w[8 + 2 * (2 + u) + 1];
       }
 #pragma unroll
       for (int e = 0; e < 8; ++e) recv[e] = __shfl_xor_sync(0xffffffffu, give[e], 1);
-      float gsum[2][7];
-      const int s0 = g * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
+      // per item: d chi^2 / d(l, m) and gB = d chi^2 / d sqrt(B); the
+      // Stokes and alpha gradients are linear in gB and follow per source
+      float gsum[2][kTaAcc];
+      const int s0 = tile_of(g) * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
         const int sl = base + 2 * i + u;
-        // rows of dJ: own row i from v, the other from recv
-        const Cx<float> o0{v[2 * sl], v[16 + 2 * sl]}, o1{v[2 * sl + 1], v[16 + 2 * sl + 1]};
+        // rows of dJ: own row i from w (source j = 2i + u), the other from recv
+        const int jo = 2 * u, jt = 2 * (2 + u);  // j for i = 0, i = 1
+        const Cx<float> o0{i ? w[jt] : w[jo], i ? w[8 + jt] : w[8 + jo]};
+        const Cx<float> o1{i ? w[jt + 1] : w[jo + 1], i ? w[8 + jt + 1] : w[8 + jo + 1]};
         const Cx<float> p0{recv[4 * u], recv[4 * u + 2]}, p1{recv[4 * u + 1], recv[4 * u + 3]};
         Jones<float> gJ;
         gJ.a = i ? p0 : o0; gJ.b = i ? p1 : o1;
         gJ.c = i ? o0 : p0; gJ.d = i ? o1 : p1;
 #pragma unroll
-        for (int k = 0; k < 7; ++k) gsum[u][k] = 0.f;
+        for (int k = 0; k < kTaAcc; ++k) gsum[u][k] = 0.f;
         if (!bad && a < A.na && sl < ns) {
-          const SrcInfo<float> src = load_source_one(A, t, ch, s0 + sl);
-          chain_item(A, t, ch, s0 + sl, a, src, sa[a], gJ, f, nu_over_c, half_log_ratio, cp, gsum[u]);
+          const SrcInfo<float> src = point_source_chain_info(A, t, ch, s0 + sl, log2_ratio);
+          Jones<float> gB;
+          chain_core(A, t, ch, s0 + sl, a, src, sa[a], gJ, f, nu_over_c, dphase, cp, gsum[u][0], gsum[u][1], gB);
+          const float* gb = reinterpret_cast<const float*>(&gB);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) gsum[u][2 + k] = gb[k];
         }
       }
       // sum over the warp's 16 antennas (lane bits 1-4), then into shared memory
 #pragma unroll
       for (int u = 0; u < 2; ++u)
 #pragma unroll
-        for (int k = 0; k < 7; ++k) {
+        for (int k = 0; k < kTaAcc; ++k) {
           float x = gsum[u][k];
           x += __shfl_xor_sync(0xffffffffu, x, 2);
           x += __shfl_xor_sync(0xffffffffu, x, 4);
           x += __shfl_xor_sync(0xffffffffu, x, 8);
           x += __shfl_xor_sync(0xffffffffu, x, 16);
-          if (lane < 2) atomicAdd(sacc + (base + 2 * i + u) * 7 + k, x);
+          if (lane < 2) atomicAdd(sacc + (base + 2 * i + u) * kTaAcc + k, x);
         }
       if (named_sync_chain_or(bad)) { bad = true; break; }
       // flush the tile's per-source sums to the FP64 accumulators
       const int ct = tid - 4 * 32;
-      if (ct < kTaKappa * 7) {
-        const int sl = ct / 7, k = ct - sl * 7, sg = s0 + sl;
-        const double val = double(sacc[ct]);
-        sacc[ct] = 0.f;
-        if (sl < ns && val != 0.0) {
-          if (k < 2) atomicAdd(&A.acc_lm[2 * sg + k], val);
-          else if (k < 6) atomicAdd(&A.acc_stokes[(size_t(sg) * A.ntime + t) * 4 + (k - 2)], val);
-          else atomicAdd(&A.acc_alpha[size_t(sg) * A.ntime + t], val);
+      if (ct < kTaKappa) {
+        const int sg = s0 + ct;
+        float* r = sacc + ct * kTaAcc;
+        if (ct < ns) {
+          if (r[0] != 0.f) atomicAdd(&A.acc_lm[2 * sg], double(r[0]));
+          if (r[1] != 0.f) atomicAdd(&A.acc_lm[2 * sg + 1], double(r[1]));
+          const SrcInfo<float> src = point_source_stokes(A, t, ch, sg, log2_ratio);
+          Jones<float> gB;
+          float* gb = reinterpret_cast<float*>(&gB);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) gb[k] = r[2 + k];
+          float gs[5];
+          stokes_grads(src, gB, half_log_ratio, gs);
+          double* st = &A.acc_stokes[(size_t(sg) * A.ntime + t) * 4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (gs[k] != 0.f) atomicAdd(st + k, double(gs[k]));
+          if (gs[4] != 0.f) atomicAdd(&A.acc_alpha[size_t(sg) * A.ntime + t], double(gs[4]));
         }
+#pragma unroll
+        for (int k = 0; k < kTaAcc; ++k) r[k] = 0.f;
       }
       named_sync_chain();
     }
@@ -1484,7 +1646,11 @@ __global__ void bsqrt_ref_kernel(FusedArgs<T> A, T* __restrict__ tab) {
     T* o = tab + kBsqVals * i;
     o[0] = B.a.r; o[1] = B.d.r; o[2] = B.b.r; o[3] = B.b.i;
     o[4] = T(0.5) * A.alpha[st];
-    o[5] = o[6] = o[7] = T(0);
+    // l / n, m / n with n = sqrt(1 - l^2 - m^2) (phase gradient), in FP64
+    const double l = A.lm[2 * s], m = A.lm[2 * s + 1], n = sqrt(1.0 - l * l - m * m);
+    o[5] = T(0);
+    o[6] = T(l / n);
+    o[7] = T(m / n);
   }
 }
 
@@ -1684,14 +1850,13 @@ mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2,
   if (A.na > 64)
     return fail(MB_ERR_UNSUPPORTED, "split-precision modes handle up to 64 antennas (got %d)", A.na);
   const int units = A.ntime * A.nchan;
-  SmemPlan S = make_plan<float>(A.na, false);
+  SmemPlan S = make_plan<float>(A.na, false, false);
   // The tensor-core kernel runs with kTcThreads threads; its extended-source
   // phase uses the same pair-tile plan with that thread count.
   S.nthreads = kTcThreads;
   S.groups = S.nitems <= kTcThreads ? std::min(8, std::max(1, kTcThreads / S.nitems)) : 1;
   TcPlan P;
   P.group = kTcGroup;
-  if (const char* g = getenv("MB_TC_GROUP")) P.group = std::max(1, atoi(g));
   // Stage buffers first (128-byte aligned), then the CUDA-core plan's regions,
   // shifted; the extended-source Jones tile reuses the stage buffers.
   const size_t stage_bytes = size_t(kTcStages) * 2 * StageGeometry<kTcRowBytes>::kMatBytes;
@@ -1773,7 +1938,7 @@ mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
     P.off_yop = take(kYopBytes);
     P.off_stage = take(size_t(kTaStages) * kJopBytes);
     P.off_ant = take(sizeof(AntInfo<float>) * A.na);
-    P.off_acc = take(sizeof(float) * kTaKappa * 7);
+    P.off_acc = take(sizeof(float) * kTaKappa * kTaAcc);
     P.off_bar = take((2 * kTaStages + 5) * sizeof(uint64_t) + 16);
     P.total = o;
     MB_CUDA(cudaFuncSetAttribute(coh_tc_adj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
