@@ -1285,14 +1285,32 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
 //   D_re = Yop Jop^T                          = Re (Y J)
 //   D_im = (-Yop_im) Jop_re^T + Yop_re Jop_im^T = Im (Y J)
 // (the second with the instruction's negate-A bit), each operand as
-// hi.hi + hi.lo + lo.hi.  Chain warps read dJ(s, a) straight from TMEM.
+// hi.hi + hi.lo + lo.hi.
+//
+// Worker warps 0-7 form two groups of four (one warp per TMEM lane quarter)
+// that take alternate tiles.  Worker lane (a, i) = TMEM lane 2a + i handles
+// the items (source 4i + u, antenna a), u = 0..3, of its group's tile: it
+// computes E, dE/dl, dE/dm, K and J once, stages J for the MMA and parks
+//   EK = E K,  Pl = dE/dl (K sqrt(B)),  Pm = dE/dm (K sqrt(B))
+// in its own TMEM lane (24 columns per item) until dJ arrives in TMEM.
+// Then, with gJ = dJ,
+//   d sqrt(B) = EK^H gJ,  d/dl_beam = Re tr(gJ^H Pl),  d/dm_beam = Re tr(gJ^H Pm),
+//   d/dphi = 2 pi nu / c * Im tr(d sqrt(B)^H sqrt(B)).
+// Lane 0 of each group's first warp issues the group's MMAs once the group
+// has staged its tile (group barrier); while one group waits for its MMAs
+// the other computes.
 constexpr int kTaRowBytes = 512;      // 256 BF16 values of K per operand row
 constexpr int kTaKappa = 8;           // sources per tile (16 operand rows)
-constexpr int kTaStages = 3;
-constexpr int kTaProducers = 128;     // warps 0-3
-constexpr int kTaChain = 256;         // warps 4-11
-constexpr int kTaThreads = kTaProducers + kTaChain + 32;  // warp 12: MMA
-constexpr uint32_t kTaCols = 64;      // 2 buffers x (D_re 16 + D_im 16)
+constexpr int kTaGroups = 3;          // worker groups = stages = TMEM regions
+constexpr int kTaGroupThreads = 128;  // 4 warps, one per TMEM lane quarter
+constexpr int kTaWorkers = kTaGroups * kTaGroupThreads;
+constexpr int kTaThreads = kTaWorkers;
+constexpr int kTaItems = 4;           // items per worker lane and tile
+// TMEM per group: 128 columns from 128 * group: D_re 16 + D_im 16, then
+// the parked item state (kTaItems x 24).
+constexpr uint32_t kTaGroupCols = 128;
+constexpr uint32_t kTaStateCol = 32;
+constexpr uint32_t kTaCols = 512;
 constexpr int kTaAcc = 10;            // per-source sums: d/dl, d/dm, gB (8)
 using TaGeom = StageGeometry<kTaRowBytes>;
 using TaLayout = StageLayout<MB_MODE_SPLIT_BF16, kTaRowBytes>;
@@ -1344,38 +1362,66 @@ __global__ void yop_build_kernel(FusedArgs<float> A) {
   }
 }
 
-__device__ __forceinline__ bool named_sync_chain_or(bool x) {
+// Barrier over the 4 warps of worker group `grp` (ids 1, 2) that ORs a
+// predicate across them.
+__device__ __forceinline__ bool group_sync_or(int grp, bool x) {
   uint32_t r;
   asm volatile(
       "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, 2, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      "bar.red.or.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
       : "=r"(r)
-      : "r"(uint32_t(x)), "n"(kTaChain)
+      : "r"(uint32_t(x)), "r"(1 + grp), "n"(kTaGroupThreads)
       : "memory");
   return r != 0;
-}
-
-__device__ __forceinline__ void named_sync_chain() {
-  asm volatile("bar.sync 2, %0;" ::"n"(kTaChain) : "memory");
 }
 
 struct TaPlan {
   size_t off_yop, off_stage, off_ant, off_acc, off_bar, total;
 };
 
-__global__ void __launch_bounds__(kTaThreads) coh_tc_adj_kernel(FusedArgs<float> A, TaPlan P) {
+// The MMAs of one tile: D_re (columns d .. d + 15) and D_im (d + 16 ..) of
+// dJ = Y J from the Y operand at ysm and the tile's J operand at jsm
+// (shared-memory addresses of the hi parts; lo parts follow).
+__device__ __forceinline__ void ta_issue_mma(uint32_t d, uint32_t ysm, uint32_t jsm) {
+  const uint32_t idesc = TaLayout::instr(128, 16);
+  const uint32_t idesc_neg = idesc | (1u << 13);  // negate A
+  const uint32_t yhi = ysm, ylo = ysm + TaGeom::kMatBytes;
+  const uint32_t jhi = jsm, jlo = jsm + kJopBytes / 2;
+  const uint32_t dre = d, dim = d + 16;
+#pragma unroll 1
+  for (int kk = 0; kk < TaGeom::kKSteps; ++kk) {
+    const uint32_t o = kk * TaGeom::kKStepBytes;
+    const uint64_t ah = TaGeom::desc(yhi + o), al = TaGeom::desc(ylo + o);
+    const uint64_t bh = TaGeom::desc(jhi + o), bl = TaGeom::desc(jlo + o);
+    TaLayout::mma(dre, ah, bh, idesc, kk == 0 ? 0u : 1u);
+    TaLayout::mma(dre, ah, bl, idesc, 1u);
+    TaLayout::mma(dre, al, bh, idesc, 1u);
+  }
+  const int half = TaGeom::kKSteps / 2;
+#pragma unroll 1
+  for (int kk = 0; kk < half; ++kk) {
+    const uint32_t ore = kk * TaGeom::kKStepBytes, oim = (kk + half) * TaGeom::kKStepBytes;
+    // D_im += (-Y_im) J_re
+    TaLayout::mma(dim, TaGeom::desc(yhi + oim), TaGeom::desc(jhi + ore), idesc_neg, kk == 0 ? 0u : 1u);
+    TaLayout::mma(dim, TaGeom::desc(yhi + oim), TaGeom::desc(jlo + ore), idesc_neg, 1u);
+    TaLayout::mma(dim, TaGeom::desc(ylo + oim), TaGeom::desc(jhi + ore), idesc_neg, 1u);
+    // D_im += Y_re J_im
+    TaLayout::mma(dim, TaGeom::desc(yhi + ore), TaGeom::desc(jhi + oim), idesc, 1u);
+    TaLayout::mma(dim, TaGeom::desc(yhi + ore), TaGeom::desc(jlo + oim), idesc, 1u);
+    TaLayout::mma(dim, TaGeom::desc(ylo + ore), TaGeom::desc(jhi + oim), idesc, 1u);
+  }
+}
+
+__global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<float> A, TaPlan P) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* syop = smem + P.off_yop;
-  unsigned char* stage = smem + P.off_stage;
+  unsigned char* stage = smem + P.off_stage;  // [kTaGroups][kJopBytes]
   AntInfo<float>* sa = reinterpret_cast<AntInfo<float>*>(smem + P.off_ant);
-  float* sacc = reinterpret_cast<float*>(smem + P.off_acc);  // [kTaKappa][kTaAcc]
+  float* sacc = reinterpret_cast<float*>(smem + P.off_acc);  // [kTaGroups][2][kTaKappa][kTaAcc]
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + P.off_bar);
-  uint64_t* full = bars;                    // [kTaStages]
-  uint64_t* empty = bars + kTaStages;       // [kTaStages]
-  uint64_t* dfull = bars + 2 * kTaStages;   // [2] MMA -> chain
-  uint64_t* dfree = dfull + 2;              // [2] chain -> MMA
-  uint64_t* done = dfree + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  uint64_t* dfull = bars;               // [kTaGroups] MMA commit -> group (dJ in TMEM)
+  uint64_t* done = dfull + kTaGroups;   // [kTaGroups] last MMAs of a group
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + kTaGroups);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -1393,20 +1439,15 @@ __global__ void __launch_bounds__(kTaThreads) coh_tc_adj_kernel(FusedArgs<float>
     for (int i = tid; i < int(kYopBytes / 16); i += blockDim.x) dst[i] = __ldg(src + i);
   }
   load_antennas(A, t, ch, sa);
-  for (int i = tid; i < kTaKappa * kTaAcc; i += blockDim.x) sacc[i] = 0.f;
+  for (int i = tid; i < kTaGroups * 2 * kTaKappa * kTaAcc; i += blockDim.x) sacc[i] = 0.f;
   if (tid == 0) {
-    for (int i = 0; i < kTaStages; ++i) {
-      tc::mbar_init(full + i, kTaProducers);
-      tc::mbar_init(empty + i, 1);
+    for (int g = 0; g < kTaGroups; ++g) {
+      tc::mbar_init(dfull + g, 1);
+      tc::mbar_init(done + g, 1);
     }
-    for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(dfull + i, 1);
-      tc::mbar_init(dfree + i, kTaChain);
-    }
-    tc::mbar_init(done, 1);
   }
   tc::fence_proxy_async_smem();
-  if (warp == 12) tc::tmem_alloc(tmem_slot, kTaCols);
+  if (warp == 0) tc::tmem_alloc(tmem_slot, kTaCols);
   tc::fence_before_thread_sync();
   __syncthreads();
   tc::fence_after_thread_sync();
@@ -1425,184 +1466,181 @@ __global__ void __launch_bounds__(kTaThreads) coh_tc_adj_kernel(FusedArgs<float>
   const int rot = int((unsigned(unit) * 2654435761u) % unsigned(max(ntiles, 1)));
   auto tile_of = [&](int g) { const int x = g + rot; return x >= ntiles ? x - ntiles : x; };
 
-  if (warp < 4) {
-    // ---- producers: J of the tile's (source, antenna) pairs into Jop ------
-    bool bad = false;
-    for (int g = 0; g < ntiles && !bad; ++g) {
-      const int slot = g % kTaStages, use = g / kTaStages;
-      if (!tc::mbar_wait(empty + slot, (use & 1) ^ 1)) { bad = true; break; }
-      const int s0 = tile_of(g) * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
-      unsigned char* hi = stage + size_t(slot) * kJopBytes;
-      unsigned char* lo = hi + kJopBytes / 2;
-#pragma unroll 1
-      for (int rep = 0; rep < 4; ++rep) {
-        // warp w, rep: antennas 4 (w + 4 rep) + (lane & 3), source lane >> 2
-        const int b = 4 * (warp + 4 * rep) + (lane & 3), sl = lane >> 2;
-        Jones<float> J = jzero<float>();
-        if (b < A.na && sl < ns) {
-          const SrcInfo<float> src = point_source_info(A, t, ch, s0 + sl, log2_ratio);
-          J = compute_jones(A, t, s0 + sl, b, src, sa[b], f, nu_over_c, cp, ch);
-        }
-        // row (s, k): K = (b, 0), (b, 1) hold J[0][k], J[1][k]
-        TaLayout::put2(hi, lo, 2 * sl, 2 * b, J.a.r, J.c.r);
-        TaLayout::put2(hi, lo, 2 * sl, 128 + 2 * b, J.a.i, J.c.i);
-        TaLayout::put2(hi, lo, 2 * sl + 1, 2 * b, J.b.r, J.d.r);
-        TaLayout::put2(hi, lo, 2 * sl + 1, 128 + 2 * b, J.b.i, J.d.i);
-      }
-      tc::fence_proxy_async_smem();
-      tc::mbar_arrive(full + slot);
-    }
-    if (bad) *abort_flag = 1;
-  } else if (warp < 12) {
-    // ---- chain warps: dJ from TMEM, chain to source parameters ------------
-    const int c = warp - 4, q = c & 3, set = c >> 2;
+  {
+    const int grp = warp >> 2, q = warp & 3;
+    const bool issuer = q == 0 && lane == 0;
+    bool issued = false;
     const int r = 32 * q + lane, a = r >> 1, i = r & 1;
-    const int base = 4 * set;               // the warp's 4 sources of a tile
+    const bool ant_ok = a < A.na;
+    const AntInfo<float> ai = sa[ant_ok ? a : 0];
+    unsigned char* hi = stage + size_t(grp) * kJopBytes;
+    unsigned char* lo = hi + kJopBytes / 2;
+    const BeamGeom G{A.lw, A.mh, A.nud};
+    const float* plane = A.plane ? A.plane + size_t(ch) * A.lw * A.mh * kPlaneVals : nullptr;
+    const uint32_t tlane = tmem + (uint32_t(32 * q) << 16) + uint32_t(kTaGroupCols * grp);
     bool bad = false;
-    for (int g = 0; g < ntiles; ++g) {
-      const int buf = g & 1;
-      if (!bad) bad = !tc::mbar_wait(dfull + buf, (g >> 1) & 1);
-      tc::fence_after_thread_sync();
-      float v[32];
-      tc::tmem_ld32(tmem + (uint32_t(32 * q) << 16) + uint32_t(32 * buf), v);
-      tc::fence_before_thread_sync();
-      tc::mbar_arrive(dfree + buf);
-      // The set's 4 sources (warp-uniform choice, constant indices):
-      // w[2j + k] = Re dJ(base + j)[i][k], w[8 + 2j + k] = Im dJ(base + j)[i][k].
-      float w[16];
-#pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        w[e] = set ? v[8 + e] : v[e];
-        w[8 + e] = set ? v[24 + e] : v[16 + e];
-      }
-      // own row i of dJ; the partner lane holds row 1 - i.  Lane i = 0
-      // chains sources j = 0, 1 of the set, lane i = 1 sources j = 2, 3: each
-      // gives the partner its row of the partner's sources.
-      float give[8], recv[8];
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        give[4 * u + 0] = i ? w[2 * u] : w[2 * (2 + u)];
-        give[4 * u + 1] = i ? w[2 * u + 1] : w[2 * (2 + u) + 1];
-        give[4 * u + 2] = i ? w[8 + 2 * u] : w[8 + 2 * (2 + u)];
-        give[4 * u + 3] = i ? w[8 + 2 * u + 1] : w[8 + 2 * (2 + u) + 1];
-      }
-#pragma unroll
-      for (int e = 0; e < 8; ++e) recv[e] = __shfl_xor_sync(0xffffffffu, give[e], 1);
-      // per item: d chi^2 / d(l, m) and gB = d chi^2 / d sqrt(B); the
-      // Stokes and alpha gradients are linear in gB and follow per source
-      float gsum[2][kTaAcc];
+    int k = 0;  // this group's tile count
+    for (int g = grp; g < ntiles; g += kTaGroups, ++k) {
       const int s0 = tile_of(g) * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
+      // ---- forward step: J of the items, staged for the MMA -------------
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int sl = base + 2 * i + u;
-        // rows of dJ: own row i from w (source j = 2i + u), the other from recv
-        const int jo = 2 * u, jt = 2 * (2 + u);  // j for i = 0, i = 1
-        const Cx<float> o0{i ? w[jt] : w[jo], i ? w[8 + jt] : w[8 + jo]};
-        const Cx<float> o1{i ? w[jt + 1] : w[jo + 1], i ? w[8 + jt + 1] : w[8 + jo + 1]};
+      for (int u = 0; u < kTaItems; ++u) {
+        const int sl = 4 * i + u;
+        Jones<float> J = jzero<float>();
+        float st[3][8];  // EK, Pl, Pm
+#pragma unroll
+        for (int e = 0; e < 8; ++e) st[0][e] = st[1][e] = st[2][e] = 0.f;
+        if (!bad && ant_ok && sl < ns) {
+          const int sg = s0 + sl;
+          const SrcInfo<float> src = point_source_info(A, t, ch, sg, log2_ratio);
+          const Cx<float> K = phase_term(A, t, sg, a, f, nu_over_c);
+          float l, m;
+          beam_lm<float>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
+          const GridPos<float> gl = grid_pos<float>(l, A.ll, A.ul, A.lscale, A.lw);
+          const GridPos<float> gm = grid_pos<float>(m, A.lmm, A.um, A.mscale, A.mh);
+          Jones<float> E, dEl, dEm;
+          if (plane) beam_interp_plane_d<float>(plane, A.mh, gl, gm, E, dEl, dEm);
+          else beam_interp_d<float>(A.E_beam, G, gl, gm, cp, E, dEl, dEm);
+          const Jones<float>& B = src.B;
+          const Jones<float> KB = {cmul(K, B.a), cmul(K, B.b), cmul(K, B.c), cmul(K, B.d)};
+          J = jmul(E, KB);
+          const Jones<float> EK = {cmul(E.a, K), cmul(E.b, K), cmul(E.c, K), cmul(E.d, K)};
+          const Jones<float> Pl = jscale(jmul(dEl, KB), gl.inside ? A.lscale : 0.f);
+          const Jones<float> Pm = jscale(jmul(dEm, KB), gm.inside ? A.mscale : 0.f);
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            st[0][e] = reinterpret_cast<const float*>(&EK)[e];
+            st[1][e] = reinterpret_cast<const float*>(&Pl)[e];
+            st[2][e] = reinterpret_cast<const float*>(&Pm)[e];
+          }
+        }
+        // park the item's state in this lane's TMEM columns (warp-collective)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) tc::tmem_st8(tlane + kTaStateCol + 24 * u + 8 * x, st[x]);
+        // row (s, k): K = (a, 0), (a, 1) hold J[0][k], J[1][k]
+        TaLayout::put2(hi, lo, 2 * sl, 2 * a, J.a.r, J.c.r);
+        TaLayout::put2(hi, lo, 2 * sl, 128 + 2 * a, J.a.i, J.c.i);
+        TaLayout::put2(hi, lo, 2 * sl + 1, 2 * a, J.b.r, J.d.r);
+        TaLayout::put2(hi, lo, 2 * sl + 1, 128 + 2 * a, J.b.i, J.d.i);
+      }
+      tc::tmem_wait_st();
+      tc::fence_proxy_async_smem();
+      tc::fence_before_thread_sync();
+      if (group_sync_or(grp, bad)) { bad = true; break; }
+      if (issuer) {
+        tc::fence_after_thread_sync();
+        ta_issue_mma(tmem + uint32_t(kTaGroupCols * grp), tc::smem_addr(syop), tc::smem_addr(hi));
+        tc::mma_commit(dfull + grp);
+        issued = true;
+      }
+      // ---- dJ of the tile: TMEM buffer grp ------------------------------
+      if (!bad) bad = !tc::mbar_wait(dfull + grp, k & 1);
+      tc::fence_after_thread_sync();
+      float v[32];  // v[2s + kc] = Re dJ(s)[i][kc], v[16 + 2s + kc] = Im
+      tc::tmem_ld32(tlane, v);
+      // own row i of dJ for sources 4i + u; the partner lane (a, 1 - i)
+      // holds row 1 - i.  Give it row i of its sources 4(1 - i) + u.
+      float recv[16];
+#pragma unroll
+      for (int u = 0; u < kTaItems; ++u)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int own = 2 * u + e, oth = 8 + 2 * u + e;  // column of source u / 4 + u
+          recv[4 * u + e] = __shfl_xor_sync(0xffffffffu, i ? v[own] : v[oth], 1);
+          recv[4 * u + 2 + e] = __shfl_xor_sync(0xffffffffu, i ? v[16 + own] : v[16 + oth], 1);
+        }
+      // ---- chain step ------------------------------------------------------
+      float* acc = sacc + (size_t(grp) * 2 + (k & 1)) * kTaKappa * kTaAcc;
+#pragma unroll
+      for (int u = 0; u < kTaItems; ++u) {
+        const int sl = 4 * i + u;
+        // own row: column 2 sl + kc of v, sl = 4i + u (constant indices, lane select)
+        const int c0 = 2 * u, c1 = 8 + 2 * u;
+        const Cx<float> o0{i ? v[c1] : v[c0], i ? v[16 + c1] : v[16 + c0]};
+        const Cx<float> o1{i ? v[c1 + 1] : v[c0 + 1], i ? v[16 + c1 + 1] : v[16 + c0 + 1]};
         const Cx<float> p0{recv[4 * u], recv[4 * u + 2]}, p1{recv[4 * u + 1], recv[4 * u + 3]};
         Jones<float> gJ;
         gJ.a = i ? p0 : o0; gJ.b = i ? p1 : o1;
         gJ.c = i ? o0 : p0; gJ.d = i ? o1 : p1;
+        float gsum[kTaAcc];
 #pragma unroll
-        for (int k = 0; k < kTaAcc; ++k) gsum[u][k] = 0.f;
-        if (!bad && a < A.na && sl < ns) {
-          const SrcInfo<float> src = point_source_chain_info(A, t, ch, s0 + sl, log2_ratio);
-          Jones<float> gB;
-          chain_core(A, t, ch, s0 + sl, a, src, sa[a], gJ, f, nu_over_c, dphase, cp, gsum[u][0], gsum[u][1], gB);
+        for (int e = 0; e < kTaAcc; ++e) gsum[e] = 0.f;
+        float sv[24];  // parked EK, Pl, Pm of the item
+        tc::tmem_ld24(tlane + kTaStateCol + 24 * u, sv);
+        if (!bad && ant_ok && sl < ns) {
+          const int sg = s0 + sl;
+          const SrcInfo<float> src = point_source_chain_info(A, t, ch, sg, log2_ratio);
+          Jones<float> EK, Pl, Pm;
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            reinterpret_cast<float*>(&EK)[e] = sv[e];
+            reinterpret_cast<float*>(&Pl)[e] = sv[8 + e];
+            reinterpret_cast<float*>(&Pm)[e] = sv[16 + e];
+          }
+          const Jones<float> gB = jhmul(EK, gJ);
+          const float g_ld = jdot_re(gJ, Pl), g_md = jdot_re(gJ, Pm);
+          // Im tr(gB^H B), B = [[a, b], [conj(b), d]] with a, d real
+          const Jones<float>& B = src.B;
+          const float imt = -gB.a.i * B.a.r - gB.d.i * B.d.r + (gB.b.r * B.b.i - gB.b.i * B.b.r) +
+                            (gB.c.r * B.c.i - gB.c.i * B.c.r);
+          const float gphi = dphase * imt;
+          gsum[0] = g_ld * ai.sc_l * ai.cos_pa + g_md * ai.sc_m * ai.sin_pa +
+                    gphi * (ai.u - ai.w * src.l_over_n);
+          gsum[1] = -g_ld * ai.sc_l * ai.sin_pa + g_md * ai.sc_m * ai.cos_pa +
+                    gphi * (ai.v - ai.w * src.m_over_n);
           const float* gb = reinterpret_cast<const float*>(&gB);
 #pragma unroll
-          for (int k = 0; k < 8; ++k) gsum[u][2 + k] = gb[k];
+          for (int e = 0; e < 8; ++e) gsum[2 + e] = gb[e];
         }
-      }
-      // sum over the warp's 16 antennas (lane bits 1-4), then into shared memory
+        // sum over the warp's 16 antennas (lane bits 1-4)
 #pragma unroll
-      for (int u = 0; u < 2; ++u)
-#pragma unroll
-        for (int k = 0; k < kTaAcc; ++k) {
-          float x = gsum[u][k];
+        for (int e = 0; e < kTaAcc; ++e) {
+          float x = gsum[e];
           x += __shfl_xor_sync(0xffffffffu, x, 2);
           x += __shfl_xor_sync(0xffffffffu, x, 4);
           x += __shfl_xor_sync(0xffffffffu, x, 8);
           x += __shfl_xor_sync(0xffffffffu, x, 16);
-          if (lane < 2) atomicAdd(sacc + (base + 2 * i + u) * kTaAcc + k, x);
+          if (lane < 2) atomicAdd(acc + sl * kTaAcc + e, x);
         }
-      if (named_sync_chain_or(bad)) { bad = true; break; }
-      // flush the tile's per-source sums to the FP64 accumulators
-      const int ct = tid - 4 * 32;
+      }
+      if (group_sync_or(grp, bad)) { bad = true; break; }
+      // flush the tile's per-source sums to the FP64 accumulators; the
+      // other accumulator buffer takes the group's next tile
+      const int ct = tid - grp * kTaGroupThreads;
       if (ct < kTaKappa) {
-        const int sg = s0 + ct;
-        float* r = sacc + ct * kTaAcc;
+        float* rr = acc + ct * kTaAcc;
         if (ct < ns) {
-          if (r[0] != 0.f) atomicAdd(&A.acc_lm[2 * sg], double(r[0]));
-          if (r[1] != 0.f) atomicAdd(&A.acc_lm[2 * sg + 1], double(r[1]));
+          const int sg = s0 + ct;
+          if (rr[0] != 0.f) atomicAdd(&A.acc_lm[2 * sg], double(rr[0]));
+          if (rr[1] != 0.f) atomicAdd(&A.acc_lm[2 * sg + 1], double(rr[1]));
           const SrcInfo<float> src = point_source_stokes(A, t, ch, sg, log2_ratio);
           Jones<float> gB;
           float* gb = reinterpret_cast<float*>(&gB);
 #pragma unroll
-          for (int k = 0; k < 8; ++k) gb[k] = r[2 + k];
+          for (int e = 0; e < 8; ++e) gb[e] = rr[2 + e];
           float gs[5];
           stokes_grads(src, gB, half_log_ratio, gs);
           double* st = &A.acc_stokes[(size_t(sg) * A.ntime + t) * 4];
 #pragma unroll
-          for (int k = 0; k < 4; ++k)
-            if (gs[k] != 0.f) atomicAdd(st + k, double(gs[k]));
+          for (int e = 0; e < 4; ++e)
+            if (gs[e] != 0.f) atomicAdd(st + e, double(gs[e]));
           if (gs[4] != 0.f) atomicAdd(&A.acc_alpha[size_t(sg) * A.ntime + t], double(gs[4]));
         }
 #pragma unroll
-        for (int k = 0; k < kTaAcc; ++k) r[k] = 0.f;
+        for (int e = 0; e < kTaAcc; ++e) rr[e] = 0.f;
       }
-      named_sync_chain();
     }
-    if (bad && c == 0 && lane == 0) *abort_flag = 1;
-  } else if (lane == 0) {
-    // ---- MMA issue ---------------------------------------------------------
-    const uint32_t idesc = TaLayout::instr(128, 16);
-    const uint32_t idesc_neg = idesc | (1u << 13);  // negate A
-    const uint32_t yhi = tc::smem_addr(syop), ylo = yhi + TaGeom::kMatBytes;
-    bool issued = false, bad = false;
-    for (int g = 0; g < ntiles; ++g) {
-      const int slot = g % kTaStages, use = g / kTaStages, buf = g & 1;
-      if (!tc::mbar_wait(full + slot, use & 1)) { bad = true; break; }
-      if (g >= 2 && !tc::mbar_wait(dfree + buf, ((g >> 1) - 1) & 1)) { bad = true; break; }
-      tc::fence_after_thread_sync();
-      const uint32_t jhi = tc::smem_addr(stage + size_t(slot) * kJopBytes), jlo = jhi + kJopBytes / 2;
-      const uint32_t dre = tmem + uint32_t(32 * buf), dim = dre + 16;
-#pragma unroll 1
-      for (int kk = 0; kk < TaGeom::kKSteps; ++kk) {
-        const uint32_t o = kk * TaGeom::kKStepBytes;
-        const uint64_t ah = TaGeom::desc(yhi + o), al = TaGeom::desc(ylo + o);
-        const uint64_t bh = TaGeom::desc(jhi + o), bl = TaGeom::desc(jlo + o);
-        TaLayout::mma(dre, ah, bh, idesc, kk == 0 ? 0u : 1u);
-        TaLayout::mma(dre, ah, bl, idesc, 1u);
-        TaLayout::mma(dre, al, bh, idesc, 1u);
-      }
-      const int half = TaGeom::kKSteps / 2;
-#pragma unroll 1
-      for (int kk = 0; kk < half; ++kk) {
-        const uint32_t ore = kk * TaGeom::kKStepBytes, oim = (kk + half) * TaGeom::kKStepBytes;
-        // D_im += (-Y_im) J_re
-        TaLayout::mma(dim, TaGeom::desc(yhi + oim), TaGeom::desc(jhi + ore), idesc_neg, kk == 0 ? 0u : 1u);
-        TaLayout::mma(dim, TaGeom::desc(yhi + oim), TaGeom::desc(jlo + ore), idesc_neg, 1u);
-        TaLayout::mma(dim, TaGeom::desc(ylo + oim), TaGeom::desc(jhi + ore), idesc_neg, 1u);
-        // D_im += Y_re J_im
-        TaLayout::mma(dim, TaGeom::desc(yhi + ore), TaGeom::desc(jhi + oim), idesc, 1u);
-        TaLayout::mma(dim, TaGeom::desc(yhi + ore), TaGeom::desc(jlo + oim), idesc, 1u);
-        TaLayout::mma(dim, TaGeom::desc(ylo + ore), TaGeom::desc(jhi + oim), idesc, 1u);
-      }
-      issued = true;
-      tc::mma_commit(empty + slot);
-      tc::mma_commit(dfull + buf);
-    }
+    // every MMA of the group has completed before TMEM is released
     if (issued) {
-      tc::mma_commit(done);
-      if (!tc::mbar_wait(done, 0)) bad = true;
+      tc::mma_commit(done + grp);
+      if (!tc::mbar_wait(done + grp, 0)) bad = true;
     }
-    if (bad) *abort_flag = 1;
+    if (bad && lane == 0) *abort_flag = 1;
   }
   tc::fence_before_thread_sync();
   __syncthreads();
   tc::fence_after_thread_sync();
-  if (warp == 12) tc::tmem_dealloc(tmem, kTaCols);
+  if (warp == 0) tc::tmem_dealloc(tmem, kTaCols);
   if (*abort_flag && tid == 0 && A.err) atomicExch(A.err, int(MB_ERR_TIMEOUT));
 }
 
@@ -1936,10 +1974,10 @@ mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
     size_t o = 0;
     auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 128); return r; };
     P.off_yop = take(kYopBytes);
-    P.off_stage = take(size_t(kTaStages) * kJopBytes);
+    P.off_stage = take(size_t(kTaGroups) * kJopBytes);
     P.off_ant = take(sizeof(AntInfo<float>) * A.na);
-    P.off_acc = take(sizeof(float) * kTaKappa * kTaAcc);
-    P.off_bar = take((2 * kTaStages + 5) * sizeof(uint64_t) + 16);
+    P.off_acc = take(sizeof(float) * kTaGroups * 2 * kTaKappa * kTaAcc);
+    P.off_bar = take(2 * kTaGroups * sizeof(uint64_t) + 16);
     P.total = o;
     MB_CUDA(cudaFuncSetAttribute(coh_tc_adj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
     {
