@@ -50,13 +50,18 @@ def rime_solver_cfg(**kwargs):
 
 
 def rime_solver(slvr_cfg):
-    """Return a RIME v4 solver for ``slvr_cfg`` (montblanc/factory.py:150-183)."""
+    """Return a RIME solver for ``slvr_cfg`` (montblanc/factory.py:150-183):
+    version 'v4' a device-resident ``RimeSolver``, version 'v5' the streaming
+    ``CompositeRimeSolver`` over host arrays."""
     version = slvr_cfg.get(Options.VERSION, Options.DEFAULT_VERSION)
     if version not in (Options.VERSION_FOUR, Options.VERSION_FIVE):
         raise ValueError('Invalid version %s (this package implements the v4 path)' % version)
     if slvr_cfg.get(Options.DATA_SOURCE) == Options.DATA_SOURCE_MS:
         raise NotImplementedError('MeasurementSet loading is not part of montblanc_gb300; '
                                   "use data_source='default', 'test' or 'empty' and transfer arrays")
+    if version == Options.VERSION_FIVE:
+        from .composite import CompositeRimeSolver
+        return CompositeRimeSolver(slvr_cfg)
     from .solver import RimeSolver
     return RimeSolver(slvr_cfg)
 
