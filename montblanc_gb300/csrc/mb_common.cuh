@@ -353,8 +353,13 @@ __device__ __forceinline__ void plane_corner(const T* __restrict__ plane, int mh
   Jones<T> e = jldg<T>(p);
   sum.a = sum.a + e.a * w; sum.b = sum.b + e.b * w;
   sum.c = sum.c + e.c * w; sum.d = sum.d + e.d * w;
-  amp[0] += w * __ldg(p + 8); amp[1] += w * __ldg(p + 9);
-  amp[2] += w * __ldg(p + 10); amp[3] += w * __ldg(p + 11);
+  if constexpr (sizeof(T) == 4) {  // 48-byte entries: |E| starts 16-byte aligned
+    const float4 ab = __ldg(reinterpret_cast<const float4*>(p + 8));
+    amp[0] += w * ab.x; amp[1] += w * ab.y; amp[2] += w * ab.z; amp[3] += w * ab.w;
+  } else {
+    amp[0] += w * __ldg(p + 8); amp[1] += w * __ldg(p + 9);
+    amp[2] += w * __ldg(p + 10); amp[3] += w * __ldg(p + 11);
+  }
 }
 
 template <typename T>

@@ -561,6 +561,15 @@ __device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, f
   named_sync_producers();
 }
 
+// Prefetch into L1 the per-item table entries of point source s at time t
+// and antenna a (sqrt(B) table, direction, FP64 path length), a tile before
+// they are read.
+__device__ __forceinline__ void prefetch_point_item(const FusedArgs<float>& A, int t, int s, int a) {
+  if (A.bsq0) tc::prefetch_l1(A.bsq0 + kBsqVals * (size_t(s) * A.ntime + t));
+  tc::prefetch_l1(A.lm + 2 * s);
+  if (A.phi) tc::prefetch_l1(A.phi + (size_t(t) * A.nsrc + s) * A.na + a);
+}
+
 // Source terms needed for a point source's J at (time t, channel ch).
 __device__ __forceinline__ SrcInfo<float> point_source_info(const FusedArgs<float>& A, int t, int ch, int s,
                                                            float log2_ratio) {
@@ -943,11 +952,19 @@ __device__ void beam_interp_plane_d(const T* __restrict__ plane, int mh, const G
     const T w = fl * fm, wl = (hl ? T(1) : T(-1)) * fm, wm = fl * (hm ? T(1) : T(-1));
     const T* p = plane + kPlaneVals * (size_t(il) * mh + im);
     Jones<T> e = jldg<T>(p);
+    T abv[4];
+    if constexpr (sizeof(T) == 4) {  // 48-byte entries: |E| starts 16-byte aligned
+      const float4 q = __ldg(reinterpret_cast<const float4*>(p + 8));
+      abv[0] = q.x; abv[1] = q.y; abv[2] = q.z; abv[3] = q.w;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) abv[k] = __ldg(p + 8 + k);
+    }
     const Cx<T>* e4 = &e.a;
     Cx<T>* s4 = &sum.a; Cx<T>* l4 = &dsl.a; Cx<T>* m4 = &dsm.a;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const T ab = __ldg(p + 8 + k);
+      const T ab = abv[k];
       s4[k] = s4[k] + e4[k] * w; amp[k] += w * ab;
       l4[k] = l4[k] + e4[k] * wl; dal[k] += wl * ab;
       m4[k] = m4[k] + e4[k] * wm; dam[k] += wm * ab;
@@ -1306,12 +1323,15 @@ constexpr int kTaGroupThreads = 128;  // 4 warps, one per TMEM lane quarter
 constexpr int kTaWorkers = kTaGroups * kTaGroupThreads;
 constexpr int kTaThreads = kTaWorkers;
 constexpr int kTaItems = 4;           // items per worker lane and tile
-// TMEM per group: 128 columns from 128 * group: D_re 16 + D_im 16, then
-// the parked item state (kTaItems x 24).
-constexpr uint32_t kTaGroupCols = 128;
-constexpr uint32_t kTaStateCol = 32;
+// TMEM per group: 160 columns from 160 * group: the two dJ accumulation
+// chains (2 x 32), then the parked item state (kTaItems x 24).
+constexpr uint32_t kTaGroupCols = 160;
+constexpr uint32_t kTaStateCol = 64;
 constexpr uint32_t kTaCols = 512;
+static_assert(kTaGroups * kTaGroupCols <= kTaCols, "TMEM columns of the worker groups");
+static_assert(kTaStateCol + kTaItems * 24 <= kTaGroupCols, "parked item state fits the group's columns");
 constexpr int kTaAcc = 10;            // per-source sums: d/dl, d/dm, gB (8)
+static_assert(kTaAcc <= 16, "per-source sums fit the 16-lane reduce-scatter");
 using TaGeom = StageGeometry<kTaRowBytes>;
 using TaLayout = StageLayout<MB_MODE_SPLIT_BF16, kTaRowBytes>;
 constexpr size_t kYopBytes = 2 * size_t(TaGeom::kMatBytes);          // hi + lo: 128 KB
@@ -1362,6 +1382,32 @@ __global__ void yop_build_kernel(FusedArgs<float> A) {
   }
 }
 
+// Sum of v[k] over the 16 lanes that share lane bit 0, by reduce-scatter
+// over lane bits 4, 3, 2, 1 (15 shuffles for 16 values).  Afterwards the
+// lane whose bits 4..1 read k holds the sum of value k; *k is returned.
+__device__ __forceinline__ float reduce_scatter16(const float (&v)[16], int lane, int* k) {
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4, b1 = lane & 2;
+  float w8[8], w4[4], w2[2];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float r = __shfl_xor_sync(0xffffffffu, b4 ? v[j] : v[j + 8], 16);
+    w8[j] = (b4 ? v[j + 8] : v[j]) + r;
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float r = __shfl_xor_sync(0xffffffffu, b3 ? w8[j] : w8[j + 4], 8);
+    w4[j] = (b3 ? w8[j + 4] : w8[j]) + r;
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const float r = __shfl_xor_sync(0xffffffffu, b2 ? w4[j] : w4[j + 2], 4);
+    w2[j] = (b2 ? w4[j + 2] : w4[j]) + r;
+  }
+  const float r = __shfl_xor_sync(0xffffffffu, b1 ? w2[0] : w2[1], 2);
+  *k = (b4 ? 8 : 0) + (b3 ? 4 : 0) + (b2 ? 2 : 0) + (b1 ? 1 : 0);
+  return (b1 ? w2[1] : w2[0]) + r;
+}
+
 // Barrier over the 4 warps of worker group `grp` (ids 1, 2) that ORs a
 // predicate across them.
 __device__ __forceinline__ bool group_sync_or(int grp, bool x) {
@@ -1379,36 +1425,36 @@ struct TaPlan {
   size_t off_yop, off_stage, off_ant, off_acc, off_bar, total;
 };
 
-// The MMAs of one tile: D_re (columns d .. d + 15) and D_im (d + 16 ..) of
-// dJ = Y J from the Y operand at ysm and the tile's J operand at jsm
-// (shared-memory addresses of the hi parts; lo parts follow).
+// The MMAs of one tile: dJ = Y J from the Y operand at ysm and the tile's J
+// operand at jsm (shared-memory addresses of the hi parts; the lo parts
+// follow, and J's lo rows sit where rows 16-31 of a 32-row operand would,
+// so one N = 32 MMA forms Y_hi [J_hi; J_lo]^T).  Per K step and chain:
+//   D[0:16] += Y_hi J_hi^T,  D[16:32] += Y_hi J_lo^T   (N = 32)
+//   D[0:16] += Y_lo J_hi^T                             (N = 16)
+// Chain Re at d + 0 (all K steps), chain Im at d + 32 (-Y_im Re J, then
+// Y_re Im J, negate-A bit for the first); dJ = D[0:16] + D[16:32] of each.
+// Descriptors advance by adding the step offset to the start-address field.
 __device__ __forceinline__ void ta_issue_mma(uint32_t d, uint32_t ysm, uint32_t jsm) {
-  const uint32_t idesc = TaLayout::instr(128, 16);
-  const uint32_t idesc_neg = idesc | (1u << 13);  // negate A
-  const uint32_t yhi = ysm, ylo = ysm + TaGeom::kMatBytes;
-  const uint32_t jhi = jsm, jlo = jsm + kJopBytes / 2;
-  const uint32_t dre = d, dim = d + 16;
-#pragma unroll 1
-  for (int kk = 0; kk < TaGeom::kKSteps; ++kk) {
-    const uint32_t o = kk * TaGeom::kKStepBytes;
-    const uint64_t ah = TaGeom::desc(yhi + o), al = TaGeom::desc(ylo + o);
-    const uint64_t bh = TaGeom::desc(jhi + o), bl = TaGeom::desc(jlo + o);
-    TaLayout::mma(dre, ah, bh, idesc, kk == 0 ? 0u : 1u);
-    TaLayout::mma(dre, ah, bl, idesc, 1u);
-    TaLayout::mma(dre, al, bh, idesc, 1u);
-  }
-  const int half = TaGeom::kKSteps / 2;
-#pragma unroll 1
+  constexpr uint32_t id32 = TaLayout::instr(128, 32), id16 = TaLayout::instr(128, 16);
+  constexpr uint32_t neg = 1u << 13;  // negate A
+  const uint64_t yh = TaGeom::desc(ysm), yl = TaGeom::desc(ysm + TaGeom::kMatBytes);
+  const uint64_t jh = TaGeom::desc(jsm);
+  constexpr uint64_t kStep = TaGeom::kKStepBytes >> 4;
+  constexpr int half = TaGeom::kKSteps / 2;
+  const uint32_t dre = d, dim = d + 32;
+#pragma unroll
   for (int kk = 0; kk < half; ++kk) {
-    const uint32_t ore = kk * TaGeom::kKStepBytes, oim = (kk + half) * TaGeom::kKStepBytes;
-    // D_im += (-Y_im) J_re
-    TaLayout::mma(dim, TaGeom::desc(yhi + oim), TaGeom::desc(jhi + ore), idesc_neg, kk == 0 ? 0u : 1u);
-    TaLayout::mma(dim, TaGeom::desc(yhi + oim), TaGeom::desc(jlo + ore), idesc_neg, 1u);
-    TaLayout::mma(dim, TaGeom::desc(ylo + oim), TaGeom::desc(jhi + ore), idesc_neg, 1u);
-    // D_im += Y_re J_im
-    TaLayout::mma(dim, TaGeom::desc(yhi + ore), TaGeom::desc(jhi + oim), idesc, 1u);
-    TaLayout::mma(dim, TaGeom::desc(yhi + ore), TaGeom::desc(jlo + oim), idesc, 1u);
-    TaLayout::mma(dim, TaGeom::desc(ylo + ore), TaGeom::desc(jhi + oim), idesc, 1u);
+    const uint64_t ore = kk * kStep, oim = (kk + half) * kStep;
+    const uint32_t acc = kk == 0 ? 0u : 1u;
+    // Re: K steps of Re J (ore) and of Im J (oim)
+    TaLayout::mma(dre, yh + ore, jh + ore, id32, acc);
+    TaLayout::mma(dim, yh + oim, jh + ore, id32 | neg, acc);
+    TaLayout::mma(dre, yl + ore, jh + ore, id16, 1u);
+    TaLayout::mma(dim, yl + oim, jh + ore, id16 | neg, 1u);
+    TaLayout::mma(dre, yh + oim, jh + oim, id32, 1u);
+    TaLayout::mma(dim, yh + ore, jh + oim, id32, 1u);
+    TaLayout::mma(dre, yl + oim, jh + oim, id16, 1u);
+    TaLayout::mma(dim, yl + ore, jh + oim, id16, 1u);
   }
 }
 
@@ -1482,6 +1528,12 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
     int k = 0;  // this group's tile count
     for (int g = grp; g < ntiles; g += kTaGroups, ++k) {
       const int s0 = tile_of(g) * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
+      if (ant_ok && g + kTaGroups < ntiles) {  // the group's next tile
+        const int sn0 = tile_of(g + kTaGroups) * kTaKappa;
+#pragma unroll
+        for (int u = 0; u < kTaItems; ++u)
+          if (sn0 + 4 * i + u < A.npsrc) prefetch_point_item(A, t, sn0 + 4 * i + u, a);
+      }
       // ---- forward step: J of the items, staged for the MMA -------------
 #pragma unroll
       for (int u = 0; u < kTaItems; ++u) {
@@ -1537,7 +1589,16 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
       if (!bad) bad = !tc::mbar_wait(dfull + grp, k & 1);
       tc::fence_after_thread_sync();
       float v[32];  // v[2s + kc] = Re dJ(s)[i][kc], v[16 + 2s + kc] = Im
-      tc::tmem_ld32(tlane, v);
+      {
+        float re[32], im[32];
+        tc::tmem_ld32(tlane, re);
+        tc::tmem_ld32(tlane + 32, im);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          v[e] = re[e] + re[16 + e];
+          v[16 + e] = im[e] + im[16 + e];
+        }
+      }
       // own row i of dJ for sources 4i + u; the partner lane (a, 1 - i)
       // holds row 1 - i.  Give it row i of its sources 4(1 - i) + u.
       float recv[16];
@@ -1562,9 +1623,9 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
         Jones<float> gJ;
         gJ.a = i ? p0 : o0; gJ.b = i ? p1 : o1;
         gJ.c = i ? o0 : p0; gJ.d = i ? o1 : p1;
-        float gsum[kTaAcc];
+        float gsum[16];  // kTaAcc values, zero padded for the reduce-scatter
 #pragma unroll
-        for (int e = 0; e < kTaAcc; ++e) gsum[e] = 0.f;
+        for (int e = 0; e < 16; ++e) gsum[e] = 0.f;
         float sv[24];  // parked EK, Pl, Pm of the item
         tc::tmem_ld24(tlane + kTaStateCol + 24 * u, sv);
         if (!bad && ant_ok && sl < ns) {
@@ -1593,15 +1654,9 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
           for (int e = 0; e < 8; ++e) gsum[2 + e] = gb[e];
         }
         // sum over the warp's 16 antennas (lane bits 1-4)
-#pragma unroll
-        for (int e = 0; e < kTaAcc; ++e) {
-          float x = gsum[e];
-          x += __shfl_xor_sync(0xffffffffu, x, 2);
-          x += __shfl_xor_sync(0xffffffffu, x, 4);
-          x += __shfl_xor_sync(0xffffffffu, x, 8);
-          x += __shfl_xor_sync(0xffffffffu, x, 16);
-          if (lane < 2) atomicAdd(acc + sl * kTaAcc + e, x);
-        }
+        int e;
+        const float x = reduce_scatter16(gsum, lane, &e);
+        if (e < kTaAcc) atomicAdd(acc + sl * kTaAcc + e, x);
       }
       if (group_sync_or(grp, bad)) { bad = true; break; }
       // flush the tile's per-source sums to the FP64 accumulators; the
