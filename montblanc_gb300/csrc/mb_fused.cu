@@ -486,23 +486,6 @@ struct TcPlan {
   int group;
 };
 
-__device__ __forceinline__ void named_sync_producers() {
-  asm volatile("bar.sync 1, %0;" ::"n"(kTcProducers) : "memory");
-}
-
-// Barrier over the producer warps that also ORs a predicate across them, so
-// that every producer takes the same branch after it.
-__device__ __forceinline__ bool named_sync_producers_or(bool x) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
-      : "=r"(r)
-      : "r"(uint32_t(x)), "n"(kTcProducers)
-      : "memory");
-  return r != 0;
-}
-
 __device__ __forceinline__ void fold_scalar(float* hi, float* lo, float x) {
   float a = *hi;
   float sum = a + x;
@@ -558,7 +541,6 @@ __device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, f
       }
     }
   }
-  named_sync_producers();
 }
 
 // Prefetch into L1 the per-item table entries of point source s at time t
@@ -686,8 +668,9 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
 
   if (warp < 8) {
     // ---- producers -------------------------------------------------------
-    // Every break below follows an OR-vote over all producers, so they leave
-    // the loop together; the MMA warp never blocks them on a barrier.
+    // No barrier joins the producer warps inside the loop: every wait is a
+    // bounded mbarrier wait, and each warp drains its own TMEM lanes into
+    // pair accumulator entries no other thread touches.
     // Item mapping: warp w covers antennas 8w .. 8w+7 and the stage's
     // sources; lane bits 0-1 and 2 pick the antenna, bits 3-4 the source.
     // Rows are written starting from row i0 = antenna bit 2, so that one
@@ -696,8 +679,8 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
     bool bad = false;
     const int a = 8 * warp + (lane & 3) + 4 * ((lane >> 2) & 1);
     const int i0 = (lane >> 2) & 1;
-    // A producer whose wait gave up skips its work but keeps taking part in
-    // the group-end votes, where all producers leave the loop together.
+    // A producer whose wait gave up (bad) skips all further waits and work;
+    // the MMA warp's waits then give up too, and everyone reaches the end.
     for (int g = 0; g < nstages; ++g) {
       const int slot = g % kTcStages, use = g / kTcStages;
       if (!bad) bad = !tc::mbar_wait(empty + slot, (use & 1) ^ 1);
@@ -727,13 +710,13 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
       if ((g % group) == group - 1 || g == nstages - 1) {
         if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1);
         tc::fence_after_thread_sync();
-        if (named_sync_producers_or(bad)) { bad = true; break; }
-        tc_drain(A, tmem, reinterpret_cast<float*>(sV), reinterpret_cast<float*>(sVlo));
+        bad = __any_sync(0xffffffffu, bad);  // the drain's TMEM loads are warp-collective
+        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), reinterpret_cast<float*>(sVlo));
         tc::fence_before_thread_sync();
-        tc::mbar_arrive(accfree);
+        if (!bad) tc::mbar_arrive(accfree);
       }
     }
-    if (bad && tid == 0) *abort_flag = 1;
+    if (bad) *abort_flag = 1;
   } else if (lane == 0) {
     // ---- MMA issue ---------------------------------------------------------
     const uint32_t idesc = L::instr(128, 128);
