@@ -102,6 +102,7 @@ def parse():
     ap.add_argument('--no-plain', action='store_true', help='skip timing the plain FP32 CUDA-core form')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-batch', action='store_true', help='skip the batched-likelihood measurement')
     ap.add_argument('--seed', type=int, default=20261203)
     return ap.parse_args()
 
@@ -226,6 +227,64 @@ def build_workload(name, seed):
     prob.arrays['observed_vis'] = model
     torch.cuda.synchronize()
     return P, prob
+
+
+def batched_likelihood(seed, nsets=256, reps=2):
+    """256 parameter sets (per-set source counts log-uniform in 10..5000,
+    point / gaussian / sersic mix) against one 100 x 27 x 64 observation:
+    chi^2 + gradient of every set per batch, the forms autotuned per set,
+    the batch captured as one CUDA graph and replayed.  Errors against the
+    FP64 form on the smallest, median and largest sets."""
+    import numpy as np
+    import torch
+    from montblanc_gb300 import synth
+    from montblanc_gb300.batch import RimeBatch, make_sets
+    from montblanc_gb300.rime import RimeProblem
+    spec = synth.WORKLOADS['medium_mixed']
+    P = synth.make_problem(**spec, seed=seed, vis_arrays=True)
+    prob = RimeProblem.from_numpy(P, dtype='float', device='cuda')
+    model = prob.empty_vis()
+    prob.forward(mode='native', model_vis=model)
+    g = torch.Generator(device='cuda')
+    g.manual_seed(seed + 1)
+    model.add_(torch.randn(model.shape, dtype=torch.complex64, device='cuda', generator=g), alpha=0.1 * math.sqrt(2.0))
+    P['observed_vis'] = model.cpu().numpy()
+    del prob, model
+    sets = make_sets(P, nsets, seed=seed + 2)
+    b = RimeBatch(P, sets, dtype='float')
+    t0 = time.time()
+    forms = b.autotune()
+    tune_s = time.time() - t0
+    b.capture()
+    b.run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        b.run()
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    x2 = b.X2.cpu().numpy()
+    n = np.array([sum(c) for c in b.counts])
+    pick = sorted({int(np.argmin(n)), int(np.argsort(n)[len(n) // 2]), int(np.argmax(n))})
+    ref = RimeBatch(P, [sets[i] for i in pick], dtype='double')
+    ref.forms = ['native'] * len(pick)
+    ref_x2 = ref.run().cpu().numpy()
+    x2_err, g_err = [], []
+    for j, i in enumerate(pick):
+        x2_err.append(abs(x2[i] - ref_x2[j]) / abs(ref_x2[j]))
+        g32, g64 = b.set_grads(i), ref.set_grads(j)
+        num = sum(float(np.sum((g32[k] - g64[k]) ** 2)) for k in ('lm', 'stokes', 'alpha'))
+        den = sum(float(np.sum(g64[k] ** 2)) for k in ('lm', 'stokes', 'alpha'))
+        g_err.append(math.sqrt(num / den))
+    return {'workload': '%d sets x (ntime 100, na 27, nchan 64), per-set nsrc log-uniform 10..5000 '
+                        '(%d sources in all), shared observation' % (nsets, int(n.sum())),
+            'sets_per_s': nsets / (ms * 1e-3), 'terms_per_s': b.terms() / (ms * 1e-3), 'ms_per_batch': ms,
+            'execution': 'one CUDA graph replay per batch (forward + adjoint of every set)',
+            'forms': {f: forms.count(f) for f in set(forms)}, 'autotune_s': tune_s,
+            'autotune_ms_by_nsrc': b.tune_times,
+            'errors_vs_fp64': {'sets': [int(n[i]) for i in pick], 'chi2_rel': x2_err, 'grad_rel_norm': g_err}}
 
 
 def subset_problem(P, prob, times, chans):
@@ -508,6 +567,8 @@ def main():
         line['e2e'] = e2e
     if not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline(P, prob)
+    if not args.no_batch:
+        line['batched'] = batched_likelihood(args.seed)
     print(json.dumps(line))
 
 
