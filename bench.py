@@ -43,9 +43,18 @@ FLOPS_FWD = 64
 FLOPS_ADJ = 128
 SM_COUNT = 152
 
-# DRAM traffic per launch of the dominant kernel from ncu captures, keyed by
-# (kernel, workload).  Captures: profiles/*.md (command lines given there).
-NCU_TRAFFIC = {}
+# DRAM traffic (bytes) per launch of the dominant kernel from ncu captures,
+# keyed by (kernel, workload, mode).
+NCU_TRAFFIC = {
+    # ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum (one pass), the
+    # timed step of `bench.py --steps 1 --warmup 1 --no-e2e --no-cpu
+    # --no-plain --no-batch` (profiles/launches_large_point_split_tf32.md)
+    ('coh_tc_adj_kernel', 'large_point', 'split_tf32'): 9.34e9 + 0.199e9,
+    ('coh_tc_fwd_kernel', 'large_point', 'split_tf32'): 6.29e9 + 3.42e9,
+    # the same with --workload profile_point (profiles/coh_tc_*_profile_point.md)
+    ('coh_tc_adj_kernel', 'profile_point', 'split_tf32'): 351.6e6 + 4.1e6,
+    ('coh_tc_fwd_kernel', 'profile_point', 'split_tf32'): 229.3e6 + 108.9e6,
+}
 
 
 def workload_terms(name):

@@ -495,49 +495,52 @@ __device__ __forceinline__ void fold_scalar(float* hi, float* lo, float x) {
   *lo += err;
 }
 
-// Whether row antenna a drains its block with column antenna b: each
-// unordered pair once, from the row whose cyclic distance to the other is
-// below na / 2 (ties: the smaller index), so every row drains about na / 2
-// columns and the producer warps share the drain evenly.
-__device__ __forceinline__ bool tc_drains(int a, int b, int na) {
-  int d = b - a;
-  if (d < 0) d += na;
-  return 2 * d < na || (2 * d == na && a < b);
-}
-
 // Drain TMEM into the float-float pair accumulators (producer threads):
 // warps 0-3 D_re, warps 4-7 D_im, each its 32 TMEM lanes (rows 2a + i).
+// Each unordered antenna pair is drained once, by the row whose cyclic
+// distance to the other is below na / 2 (ties: the smaller index), so every
+// row drains about na / 2 columns and the warps share the work evenly: row a
+// drains the antennas b of the cyclic interval [a, a + dmax], b in
+// [a, up_hi] from its own block of V_ab and the wrapped b in [0, wrap_end]
+// as V_ba = (sum J_a J_b^H)^H (transposed, conjugated).
+// Element offsets of the pair accumulators (pair_index(p, q) * 8 + (2 row +
+// col) * 2 + re/im) split into a per-lane part and a part in b and j:
+//   b >= a:  ku + 8 b + 2 j,  ku = 8 (a na - a (a - 1) / 2 - a) + 4 i + h
+//   b <  a:  8 R_b + kl + 4 j,  kl = 8 a + 2 i + h,  R_b = b na - b (b - 1) / 2 - b
 __device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, float* sVlof) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int q = warp & 3, h = warp >> 2;
   const int r = 32 * q + lane, a = r >> 1, i = r & 1;
   const int na = A.na;
   const bool row_ok = a < na;
-  const int dmax = (na - 1) / 2 + ((na % 2 == 0 && a < na / 2) ? 1 : 0);  // drained b: a .. a + dmax (cyclic)
+  const int dmax = (na - 1) / 2 + ((na % 2 == 0 && a < na / 2) ? 1 : 0);
+  const int up_hi = row_ok ? min(a + dmax, na - 1) : -1;
+  const int wrap_end = row_ok ? a + dmax - na : -1;
+  const int ku = 8 * (a * na - (a * (a - 1)) / 2 - a) + 4 * i + h;
+  const int kl = 8 * a + 2 * i + h;
+  const float sgn = h ? -1.f : 1.f;
   const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(h * 128);
-  for (int c0 = 0; c0 < 128; c0 += 32) {
-    const int b_lo = c0 >> 1, b_hi = min(b_lo + 15, na - 1);
-    // does the cyclic interval [a, a + dmax] meet [b_lo, b_hi]?  (warp-uniform skip)
-    int x = b_lo - a, y = a - b_lo;
-    if (x < 0) x += na;
-    if (y < 0) y += na;
-    const bool meets = row_ok && b_lo < na && (x <= dmax || y <= b_hi - b_lo);
-    if (!__any_sync(0xffffffffu, meets)) continue;
+#pragma unroll 1
+  for (int blk = 0; blk < 4; ++blk) {
+    const int b_lo = 16 * blk;
+    const bool need = (max(a, b_lo) <= min(up_hi, b_lo + 15)) || (wrap_end >= b_lo);
+    if (!__any_sync(0xffffffffu, need)) continue;  // warp-uniform: the loads are collective
     float v[32], w[32];
-    tc::tmem_ld32(lane_addr + c0, v);
-    tc::tmem_ld32(lane_addr + 256 + c0, w);
-    if (!meets) continue;
+    tc::tmem_ld32x2(lane_addr + 32 * blk, lane_addr + 256 + 32 * blk, v, w);
 #pragma unroll
-    for (int c = 0; c < 32; ++c) {
-      const int n = c0 + c, b = n >> 1, j = n & 1;
-      if (b >= na || !tc_drains(a, b, na)) continue;
-      const float val = v[c] + w[c];
-      if (a <= b) {
-        const int e = pair_index(a, b, na) * 8 + (2 * i + j) * 2 + h;  // h = 0: re, 1: im
-        fold_scalar(sVf + e, sVlof + e, val);
-      } else {  // V_ba = (sum J_a J_b^H)^H: transpose, conjugate
-        const int e = pair_index(b, a, na) * 8 + (2 * j + i) * 2 + h;
-        fold_scalar(sVf + e, sVlof + e, h ? -val : val);
+    for (int k = 0; k < 32; ++k) v[k] += w[k];  // main + correction accumulators
+    if (!need) continue;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const int b = b_lo + c;
+      if (b >= a && b <= up_hi) {
+        const int e = ku + 8 * b;
+        fold_scalar(sVf + e, sVlof + e, v[2 * c]);
+        fold_scalar(sVf + e + 2, sVlof + e + 2, v[2 * c + 1]);
+      } else if (b <= wrap_end) {
+        const int e = 8 * (b * na - (b * (b - 1)) / 2 - b) + kl;
+        fold_scalar(sVf + e, sVlof + e, sgn * v[2 * c]);
+        fold_scalar(sVf + e + 4, sVlof + e + 4, sgn * v[2 * c + 1]);
       }
     }
   }
