@@ -48,10 +48,10 @@ SM_COUNT = 152
 NCU_TRAFFIC = {
     # ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum (one pass), the
     # timed step of `bench.py --steps 1 --warmup 1 --no-e2e --no-cpu
-    # --no-plain --no-batch` (profiles/launches_large_point_split_tf32.md)
+    # --no-plain --no-batch`
     ('coh_tc_adj_kernel', 'large_point', 'split_tf32'): 9.34e9 + 0.199e9,
     ('coh_tc_fwd_kernel', 'large_point', 'split_tf32'): 6.29e9 + 3.42e9,
-    # the same with --workload profile_point (profiles/coh_tc_*_profile_point.md)
+    # the same with --workload profile_point
     ('coh_tc_adj_kernel', 'profile_point', 'split_tf32'): 351.6e6 + 4.1e6,
     ('coh_tc_fwd_kernel', 'profile_point', 'split_tf32'): 229.3e6 + 108.9e6,
 }
