@@ -221,7 +221,10 @@ mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
  * A (128 x K) . B (128 x K)^T for row-major FP32 device arrays, computed
  * with the split-precision tensor-core operand path of the fused kernels
  * (mode MB_MODE_SPLIT_TF32: K % 32 == 0; MB_MODE_SPLIT_BF16: K % 64 == 0).
+ * With mode MB_MODE_SPLIT_BF16 | MB_TC_SELFTEST_A_IN_TMEM the A operand is
+ * read from tensor memory (as the split-precision adjoint reads dchi^2/dV).
  * *status (device int) is set to 1 if a bounded wait gave up. */
+#define MB_TC_SELFTEST_A_IN_TMEM 0x10
 mb_status mb_tc_selftest(const float* A, const float* B, int K, int mode,
                          float* D, int* status, void* stream);
 

@@ -28,6 +28,7 @@ MB_MODE_NATIVE, MB_MODE_SPLIT_TF32, MB_MODE_SPLIT_BF16 = 0, 1, 2
 MODES = {'native': MB_MODE_NATIVE, 'split_tf32': MB_MODE_SPLIT_TF32, 'split_bf16': MB_MODE_SPLIT_BF16}
 MB_APPLY_WEIGHTS = 0x1
 MB_RESIDUALS = 0x2
+MB_TC_SELFTEST_A_IN_TMEM = 0x10
 
 DIM_NAMES = ('ntime', 'na', 'nbl', 'nchan', 'npol', 'npolchan', 'nsrc', 'npsrc', 'ngsrc', 'nssrc',
              'beam_lw', 'beam_mh', 'beam_nud')

@@ -204,8 +204,9 @@ __device__ __forceinline__ Jones<T> brightness_sqrt(T I, T Q, T U, T V, T power)
 
 // ---- phase (a2) ----------------------------------------------------------
 // K = exp(-2 pi i phi nu / c), phi = u l + v m + w (n - 1).  The phase
-// argument and its range reduction are always evaluated in FP64
-// (CPUSolver.py:162-195).
+// argument is always formed in FP64 (CPUSolver.py:162-195); in the FP32
+// forms its reduction to [-1/2, 1/2] cycles is exact on that FP64 value
+// (fp64_frac_nearest) and only the reduced argument is rounded to FP32.
 template <typename T> __device__ __forceinline__ Cx<T> phase_from_phi(double phi, double freq);
 // FP64: exp(i * ((-2 pi phi) nu) / c), in the oracle's evaluation order.
 template <> __device__ __forceinline__ Cx<double> phase_from_phi<double>(double phi, double freq) {
@@ -214,13 +215,13 @@ template <> __device__ __forceinline__ Cx<double> phase_from_phi<double>(double 
   sincos(arg, &s, &c);
   return {c, s};
 }
-// FP32: cycles = phi nu / c and its fractional part in FP64, then an FP32
+// FP32: cycles = phi nu / c in FP64 and its exact reduction, then an FP32
 // sincospi of the reduced argument.
+__device__ __forceinline__ float fp64_frac_nearest(double x);
 template <> __device__ __forceinline__ Cx<float> phase_from_phi<float>(double phi, double freq) {
-  double cycles = phi * freq / kLightSpeed;
-  double frac = cycles - rint(cycles);
+  const float frac = fp64_frac_nearest(phi * freq / kLightSpeed);
   float s, c;
-  sincospif(-2.0f * static_cast<float>(frac), &s, &c);
+  sincospif(-2.0f * frac, &s, &c);
   return {c, s};
 }
 
@@ -233,11 +234,31 @@ template <> __device__ __forceinline__ Cx<double> phase_from_cycles<double>(doub
   sincospi(-2.0 * frac, &s, &c);
   return {c, s};
 }
+// r = x - rint(x) for an FP64 x, rounded to FP32 (a tie may come out as
+// +1/2 or -1/2; both give the same phase factor).  The reduction is exact:
+// it keeps the bits of x's 53-bit significand below the binary point,
+// working on the bit pattern with integer instructions, so the only FP64
+// instruction of the phase is the product forming x.
+__device__ __forceinline__ float fp64_frac_nearest(double x) {
+  const long long bits = __double_as_longlong(x);
+  const int ex = int((bits >> 52) & 0x7ff);
+  if (ex == 0x7ff) return __int_as_float(0x7fc00000);  // NaN / inf input stays NaN
+  const int f = 1075 - ex;               // fraction bits of the significand
+  if (ex == 0 || f <= 0) return 0.f;     // zero or subnormal, or an integer
+  if (f > 62) return float(x);           // |x| < 2^-9: nothing to reduce
+  const long long m = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+  long long fb = m & ((1LL << f) - 1);
+  if (fb >= (1LL << (f - 1))) fb -= (1LL << f);
+  if (bits < 0) fb = -fb;
+  const int sh = f > 31 ? f - 31 : 0;     // keep 31 bits: |fb >> sh| <= 2^30
+  const int r32 = int(fb >> sh);
+  return float(r32) * __int_as_float((127 + sh - f) << 23);  // * 2^(sh - f), exact
+}
+
 template <> __device__ __forceinline__ Cx<float> phase_from_cycles<float>(double phi, double nu_over_c) {
-  double cycles = phi * nu_over_c;
-  double frac = cycles - rint(cycles);
+  const float frac = fp64_frac_nearest(phi * nu_over_c);
   float s, c;
-  sincospif(-2.0f * static_cast<float>(frac), &s, &c);
+  sincospif(-2.0f * frac, &s, &c);
   return {c, s};
 }
 

@@ -34,6 +34,31 @@ def test_split_gemm_selftest(mode, K, tol):
     assert np.isfinite(got).all()
 
 
+@pytest.mark.parametrize('K', [64, 256])
+def test_split_gemm_selftest_a_in_tmem(K):
+    """BF16 split product with the A operand read from tensor memory equals
+    the same product with A from shared memory (and the FP64 product)."""
+    import torch
+    from montblanc_gb300 import _cabi
+    g = torch.Generator(device='cpu').manual_seed(K + 1)
+    A32 = torch.randn(128, K, generator=g, dtype=torch.float64).float().cuda()
+    B32 = torch.randn(128, K, generator=g, dtype=torch.float64).float().cuda()
+    out = {}
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for flag in (0, _cabi.MB_TC_SELFTEST_A_IN_TMEM):
+        D = torch.zeros(128, 128, dtype=torch.float32, device='cuda')
+        status = torch.zeros(1, dtype=torch.int32, device='cuda')
+        _cabi.call('mb_tc_selftest', A32.data_ptr(), B32.data_ptr(), K, _cabi.MODES['split_bf16'] | flag,
+                   D.data_ptr(), status.data_ptr(), stream)
+        torch.cuda.synchronize()
+        assert status.item() == 0
+        out[flag] = D.cpu().double().numpy()
+    ref = (A32.double().cpu() @ B32.double().cpu().T).numpy()
+    got = out[_cabi.MB_TC_SELFTEST_A_IN_TMEM]
+    assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 5e-5
+    assert np.max(np.abs(got - out[0])) <= 1e-6 * np.max(np.abs(ref))
+
+
 SPLIT_TOL = {'split_tf32': {'vis': 2e-5, 'terms': 1e-3, 'X2': 1e-4},
              'split_bf16': {'vis': 2e-4, 'terms': 1e-2, 'X2': 1e-3}}
 
