@@ -1280,7 +1280,9 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
 // Split-precision adjoint: dJ = Y J for point sources on the tensor cores
 // ---------------------------------------------------------------------------
 // Y (2na x 2na complex, rows (a, i), columns (b, j)) is the Hermitian matrix
-// of d chi^2 / dV.  As a real operand (128 rows x 256 K, BF16 hi + lo):
+// of d chi^2 / dV.  As a real operand (128 rows x 256 K, BF16 hi + lo), held
+// in TMEM as the MMAs' A operand (columns 0-127 hi, 128-255 lo, two K values
+// per column):
 //   Yop[(a,i), (b,j)] = Re Y_ab[i][j],  Yop[(a,i), 128 + (b,j)] = -Im Y_ab[i][j].
 // Per tile of kTaKappa sources the producers stage
 //   Jop[(s,k), (b,j)] = Re J_sb[j][k],  Jop[(s,k), 128 + (b,j)] = Im J_sb[j][k]
@@ -1295,7 +1297,7 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
 // the items (source 4i + u, antenna a), u = 0..3, of its group's tile: it
 // computes E, dE/dl, dE/dm, K and J once, stages J for the MMA and parks
 //   EK = E K,  Pl = dE/dl (K sqrt(B)),  Pm = dE/dm (K sqrt(B))
-// in its own TMEM lane (24 columns per item) until dJ arrives in TMEM.
+// in shared memory (6 float4 per item) until dJ arrives in TMEM.
 // Then, with gJ = dJ,
 //   d sqrt(B) = EK^H gJ,  d/dl_beam = Re tr(gJ^H Pl),  d/dm_beam = Re tr(gJ^H Pm),
 //   d/dphi = 2 pi nu / c * Im tr(d sqrt(B)^H sqrt(B)).
@@ -1309,13 +1311,13 @@ constexpr int kTaGroupThreads = 128;  // 4 warps, one per TMEM lane quarter
 constexpr int kTaWorkers = kTaGroups * kTaGroupThreads;
 constexpr int kTaThreads = kTaWorkers;
 constexpr int kTaItems = 4;           // items per worker lane and tile
-// TMEM per group: 160 columns from 160 * group: the two dJ accumulation
-// chains (2 x 32), then the parked item state (kTaItems x 24).
-constexpr uint32_t kTaGroupCols = 160;
-constexpr uint32_t kTaStateCol = 64;
+// TMEM: the Y operand in columns 0-255, then per group the two dJ
+// accumulation chains (2 x 32 columns) from kTaYCols + 64 * group.
+constexpr uint32_t kTaYCols = 256;
+constexpr uint32_t kTaGroupCols = 64;
 constexpr uint32_t kTaCols = 512;
-static_assert(kTaGroups * kTaGroupCols <= kTaCols, "TMEM columns of the worker groups");
-static_assert(kTaStateCol + kTaItems * 24 <= kTaGroupCols, "parked item state fits the group's columns");
+static_assert(kTaYCols + kTaGroups * kTaGroupCols <= kTaCols, "TMEM columns of Y and the worker groups");
+constexpr int kTaPark = 6;            // float4 of parked state per item
 constexpr int kTaAcc = 10;            // per-source sums: d/dl, d/dm, gB (8)
 static_assert(kTaAcc <= 16, "per-source sums fit the 16-lane reduce-scatter");
 using TaGeom = StageGeometry<kTaRowBytes>;
@@ -1342,9 +1344,9 @@ __global__ void yop_build_kernel(FusedArgs<float> A) {
     atomic_add_jones(&sY[q * na + p], jherm(g));
   }
   __syncthreads();
-  unsigned char* hi = A.yop + size_t(unit) * kYopBytes;
-  unsigned char* lo = hi + TaGeom::kMatBytes;
-  // element pairs (row r, K = 2kp, 2kp + 1): j = 0, 1 of antenna b
+  // row r: 128 words of hi parts, then 128 words of lo parts; word kp holds
+  // K = 2kp (low half) and 2kp + 1: j = 0, 1 of antenna b
+  uint32_t* yw = reinterpret_cast<uint32_t*>(A.yop + size_t(unit) * kYopBytes);
   for (int idx = threadIdx.x; idx < 128 * 128; idx += blockDim.x) {
     const int r = idx >> 7, kp = idx & 127;
     const int a = r >> 1, i = r & 1;
@@ -1360,11 +1362,8 @@ __global__ void yop_build_kernel(FusedArgs<float> A) {
     __nv_bfloat16 h0, l0, h1, l1;
     tc::split_bf16(x0, h0, l0);
     tc::split_bf16(x1, h1, l1);
-    const uint32_t o = TaGeom::offset(r, 2 * (2 * kp));
-    __nv_bfloat162 hh, ll;
-    hh.x = h0; hh.y = h1; ll.x = l0; ll.y = l1;
-    *reinterpret_cast<__nv_bfloat162*>(hi + o) = hh;
-    *reinterpret_cast<__nv_bfloat162*>(lo + o) = ll;
+    yw[r * 256 + kp] = uint32_t(__bfloat16_as_ushort(h0)) | (uint32_t(__bfloat16_as_ushort(h1)) << 16);
+    yw[r * 256 + 128 + kp] = uint32_t(__bfloat16_as_ushort(l0)) | (uint32_t(__bfloat16_as_ushort(l1)) << 16);
   }
 }
 
@@ -1408,45 +1407,46 @@ __device__ __forceinline__ bool group_sync_or(int grp, bool x) {
 }
 
 struct TaPlan {
-  size_t off_yop, off_stage, off_ant, off_acc, off_bar, total;
+  size_t off_park, off_stage, off_ant, off_acc, off_bar, total;
 };
 
-// The MMAs of one tile: dJ = Y J from the Y operand at ysm and the tile's J
-// operand at jsm (shared-memory addresses of the hi parts; the lo parts
-// follow, and J's lo rows sit where rows 16-31 of a 32-row operand would,
-// so one N = 32 MMA forms Y_hi [J_hi; J_lo]^T).  Per K step and chain:
+// The MMAs of one tile: dJ = Y J from the Y operand in TMEM (ytm: column 0,
+// lane 0) and the tile's J operand at jsm (shared-memory address of the hi
+// part; the lo part follows, and J's lo rows sit where rows 16-31 of a 32-row
+// operand would, so one N = 32 MMA forms Y_hi [J_hi; J_lo]^T).  Per K step
+// (16 values: 8 TMEM columns of Y) and chain:
 //   D[0:16] += Y_hi J_hi^T,  D[16:32] += Y_hi J_lo^T   (N = 32)
 //   D[0:16] += Y_lo J_hi^T                             (N = 16)
 // Chain Re at d + 0 (all K steps), chain Im at d + 32 (-Y_im Re J, then
 // Y_re Im J, negate-A bit for the first); dJ = D[0:16] + D[16:32] of each.
-// Descriptors advance by adding the step offset to the start-address field.
-__device__ __forceinline__ void ta_issue_mma(uint32_t d, uint32_t ysm, uint32_t jsm) {
+__device__ __forceinline__ void ta_issue_mma(uint32_t d, uint32_t ytm, uint32_t jsm) {
   constexpr uint32_t id32 = TaLayout::instr(128, 32), id16 = TaLayout::instr(128, 16);
   constexpr uint32_t neg = 1u << 13;  // negate A
-  const uint64_t yh = TaGeom::desc(ysm), yl = TaGeom::desc(ysm + TaGeom::kMatBytes);
+  const uint32_t yh = ytm, yl = ytm + 128;
   const uint64_t jh = TaGeom::desc(jsm);
   constexpr uint64_t kStep = TaGeom::kKStepBytes >> 4;
   constexpr int half = TaGeom::kKSteps / 2;
   const uint32_t dre = d, dim = d + 32;
 #pragma unroll
   for (int kk = 0; kk < half; ++kk) {
-    const uint64_t ore = kk * kStep, oim = (kk + half) * kStep;
+    const uint64_t ore = kk * kStep, oim = (kk + half) * kStep;  // J descriptor steps
+    const uint32_t cre = 8 * kk, cim = 8 * (kk + half);          // Y columns
     const uint32_t acc = kk == 0 ? 0u : 1u;
     // Re: K steps of Re J (ore) and of Im J (oim)
-    TaLayout::mma(dre, yh + ore, jh + ore, id32, acc);
-    TaLayout::mma(dim, yh + oim, jh + ore, id32 | neg, acc);
-    TaLayout::mma(dre, yl + ore, jh + ore, id16, 1u);
-    TaLayout::mma(dim, yl + oim, jh + ore, id16 | neg, 1u);
-    TaLayout::mma(dre, yh + oim, jh + oim, id32, 1u);
-    TaLayout::mma(dim, yh + ore, jh + oim, id32, 1u);
-    TaLayout::mma(dre, yl + oim, jh + oim, id16, 1u);
-    TaLayout::mma(dim, yl + ore, jh + oim, id16, 1u);
+    tc::mma_f16_ta(dre, yh + cre, jh + ore, id32, acc);
+    tc::mma_f16_ta(dim, yh + cim, jh + ore, id32 | neg, acc);
+    tc::mma_f16_ta(dre, yl + cre, jh + ore, id16, 1u);
+    tc::mma_f16_ta(dim, yl + cim, jh + ore, id16 | neg, 1u);
+    tc::mma_f16_ta(dre, yh + cim, jh + oim, id32, 1u);
+    tc::mma_f16_ta(dim, yh + cre, jh + oim, id32, 1u);
+    tc::mma_f16_ta(dre, yl + cim, jh + oim, id16, 1u);
+    tc::mma_f16_ta(dim, yl + cre, jh + oim, id16, 1u);
   }
 }
 
 __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<float> A, TaPlan P) {
   extern __shared__ __align__(16) unsigned char smem[];
-  unsigned char* syop = smem + P.off_yop;
+  float4* park = reinterpret_cast<float4*>(smem + P.off_park);  // [group][item][kTaPark][128 lanes]
   unsigned char* stage = smem + P.off_stage;  // [kTaGroups][kJopBytes]
   AntInfo<float>* sa = reinterpret_cast<AntInfo<float>*>(smem + P.off_ant);
   float* sacc = reinterpret_cast<float*>(smem + P.off_acc);  // [kTaGroups][2][kTaKappa][kTaAcc]
@@ -1464,12 +1464,6 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
   if (*abort_flag) return;
   __syncthreads();
 
-  // Y operand of this unit: 128 KB, 16-byte vector copies
-  {
-    const uint4* src = reinterpret_cast<const uint4*>(A.yop + size_t(unit) * kYopBytes);
-    uint4* dst = reinterpret_cast<uint4*>(syop);
-    for (int i = tid; i < int(kYopBytes / 16); i += blockDim.x) dst[i] = __ldg(src + i);
-  }
   load_antennas(A, t, ch, sa);
   for (int i = tid; i < kTaGroups * 2 * kTaKappa * kTaAcc; i += blockDim.x) sacc[i] = 0.f;
   if (tid == 0) {
@@ -1484,6 +1478,26 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
   __syncthreads();
   tc::fence_after_thread_sync();
   const uint32_t tmem = *tmem_slot;
+  // Y operand of this unit into TMEM columns 0-255: row r = TMEM lane r;
+  // the three warps of a lane quarter share the row's 8 runs of 32 words.
+  {
+    const int q = warp & 3, part = warp >> 2;
+    const int r = 32 * q + lane;
+    const uint4* src = reinterpret_cast<const uint4*>(A.yop + size_t(unit) * kYopBytes) + r * 64;
+    for (int run = part; run < 8; run += kTaGroups) {
+      uint32_t w[32];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const uint4 x = __ldg(src + 8 * run + k);
+        w[4 * k] = x.x; w[4 * k + 1] = x.y; w[4 * k + 2] = x.z; w[4 * k + 3] = x.w;
+      }
+      tc::tmem_st32(tmem + (uint32_t(32 * q) << 16) + uint32_t(32 * run), w);
+    }
+    tc::tmem_wait_st();
+  }
+  tc::fence_before_thread_sync();
+  __syncthreads();
+  tc::fence_after_thread_sync();
 
   const float f = A.freq[ch];
   const double nu_over_c = double(f) / kLightSpeed;
@@ -1509,7 +1523,8 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
     unsigned char* lo = hi + kJopBytes / 2;
     const BeamGeom G{A.lw, A.mh, A.nud};
     const float* plane = A.plane ? A.plane + size_t(ch) * A.lw * A.mh * kPlaneVals : nullptr;
-    const uint32_t tlane = tmem + (uint32_t(32 * q) << 16) + uint32_t(kTaGroupCols * grp);
+    const uint32_t tlane = tmem + (uint32_t(32 * q) << 16) + kTaYCols + uint32_t(kTaGroupCols * grp);
+    float4* mypark = park + size_t(grp) * kTaItems * kTaPark * 128 + r;
     bool bad = false;
     int k = 0;  // this group's tile count
     for (int g = grp; g < ntiles; g += kTaGroups, ++k) {
@@ -1552,22 +1567,24 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
             st[2][e] = reinterpret_cast<const float*>(&Pm)[e];
           }
         }
-        // park the item's state in this lane's TMEM columns (warp-collective)
+        // park the item's state in shared memory (lane-contiguous float4)
 #pragma unroll
-        for (int x = 0; x < 3; ++x) tc::tmem_st8(tlane + kTaStateCol + 24 * u + 8 * x, st[x]);
+        for (int x = 0; x < 3; ++x) {
+          mypark[(u * kTaPark + 2 * x) * 128] = make_float4(st[x][0], st[x][1], st[x][2], st[x][3]);
+          mypark[(u * kTaPark + 2 * x + 1) * 128] = make_float4(st[x][4], st[x][5], st[x][6], st[x][7]);
+        }
         // row (s, k): K = (a, 0), (a, 1) hold J[0][k], J[1][k]
         TaLayout::put2(hi, lo, 2 * sl, 2 * a, J.a.r, J.c.r);
         TaLayout::put2(hi, lo, 2 * sl, 128 + 2 * a, J.a.i, J.c.i);
         TaLayout::put2(hi, lo, 2 * sl + 1, 2 * a, J.b.r, J.d.r);
         TaLayout::put2(hi, lo, 2 * sl + 1, 128 + 2 * a, J.b.i, J.d.i);
       }
-      tc::tmem_wait_st();
       tc::fence_proxy_async_smem();
       tc::fence_before_thread_sync();
       if (group_sync_or(grp, bad)) { bad = true; break; }
       if (issuer) {
         tc::fence_after_thread_sync();
-        ta_issue_mma(tmem + uint32_t(kTaGroupCols * grp), tc::smem_addr(syop), tc::smem_addr(hi));
+        ta_issue_mma(tmem + kTaYCols + uint32_t(kTaGroupCols * grp), tmem, tc::smem_addr(hi));
         tc::mma_commit(dfull + grp);
         issued = true;
       }
@@ -1613,7 +1630,11 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
 #pragma unroll
         for (int e = 0; e < 16; ++e) gsum[e] = 0.f;
         float sv[24];  // parked EK, Pl, Pm of the item
-        tc::tmem_ld24(tlane + kTaStateCol + 24 * u, sv);
+#pragma unroll
+        for (int x = 0; x < kTaPark; ++x) {
+          const float4 p4 = mypark[(u * kTaPark + x) * 128];
+          sv[4 * x] = p4.x; sv[4 * x + 1] = p4.y; sv[4 * x + 2] = p4.z; sv[4 * x + 3] = p4.w;
+        }
         if (!bad && ant_ok && sl < ns) {
           const int sg = s0 + sl;
           const SrcInfo<float> src = point_source_chain_info(A, t, ch, sg, log2_ratio);
@@ -2014,7 +2035,7 @@ mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
     TaPlan P;
     size_t o = 0;
     auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 128); return r; };
-    P.off_yop = take(kYopBytes);
+    P.off_park = take(sizeof(float4) * kTaGroups * kTaItems * kTaPark * 128);
     P.off_stage = take(size_t(kTaGroups) * kJopBytes);
     P.off_ant = take(sizeof(AntInfo<float>) * A.na);
     P.off_acc = take(sizeof(float) * kTaGroups * 2 * kTaKappa * kTaAcc);
