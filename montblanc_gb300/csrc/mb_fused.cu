@@ -473,16 +473,29 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A,
 // accumulations into one accumulator (about 2.5e-8 of the result per
 // accumulation for a coherent sum); short groups keep the sum over all
 // sources near 1e-7 relative.
-constexpr int kTcProducers = 256;          // warps 0-7: operands, TMEM drain
-constexpr int kTcThreads = kTcProducers + 32;  // warp 8: MMA issue
+constexpr int kTcProducerWarps = 11;       // warps 0-10: operands (one source each), drain
+constexpr int kTcProducers = 32 * kTcProducerWarps;
+constexpr int kTcThreads = kTcProducers + 32;  // warp 11: MMA issue, drain
 constexpr int kTcStages = 2;
-constexpr int kTcRowBytes = 128;  // 8 sources (TF32) / 16 sources (BF16) per stage
-constexpr int kTcGroup = 8;                // stages per TMEM accumulation group
+constexpr int kTcGroup = 5;                // stages per TMEM accumulation group (55 sources)
 // TMEM columns: D_re 0-127, D_im 128-255 (hi.hi); their corrections 256-511.
 constexpr uint32_t kTcCols = 512;
 
+// Stage geometry: kSlots source slots per stage (the producer warps fill
+// kTcProducerWarps of them, the rest stay zero), so that the K values of the
+// real and of the imaginary parts (2 kSlots each) fill whole MMA K steps.
+template <int MODE> struct TcGeom;
+template <> struct TcGeom<MB_MODE_SPLIT_TF32> {
+  static constexpr int kSlots = 12, kRowBytes = kSlots * 4 * 4;  // 6 K steps of 8
+};
+template <> struct TcGeom<MB_MODE_SPLIT_BF16> {
+  static constexpr int kSlots = 16, kRowBytes = kSlots * 4 * 2;  // 4 K steps of 16
+};
+static_assert(TcGeom<MB_MODE_SPLIT_TF32>::kSlots >= kTcProducerWarps, "a slot per producer warp");
+static_assert(TcGeom<MB_MODE_SPLIT_BF16>::kSlots >= kTcProducerWarps, "a slot per producer warp");
+
 struct TcPlan {
-  size_t off_stage, off_bar, total;
+  size_t off_stage, off_vlo16, off_vlo32, off_bar, total;
   int group;
 };
 
@@ -495,8 +508,21 @@ __device__ __forceinline__ void fold_scalar(float* hi, float* lo, float x) {
   *lo += err;
 }
 
-// Drain TMEM into the float-float pair accumulators (producer threads):
-// warps 0-3 D_re, warps 4-7 D_im, each its 32 TMEM lanes (rows 2a + i).
+// The same with the low part kept in BF16: it only carries the rounding
+// errors of the high part (a few ulp of it), which 8 significant bits hold
+// to far below an ulp of the sum.
+__device__ __forceinline__ void fold_scalar(float* hi, __nv_bfloat16* lo, float x) {
+  float a = *hi;
+  float sum = a + x;
+  float bp = sum - a;
+  float err = (a - (sum - bp)) + (x - bp);
+  *hi = sum;
+  *lo = __float2bfloat16_rn(__bfloat162float(*lo) + err);
+}
+
+// Drain TMEM into the float-float pair accumulators (all 12 warps): a warp
+// reads the 32 TMEM lanes of its quarter (rows 2a + i) and takes every third
+// of the quarter's 8 tasks (D_re or D_im, one block of 16 column antennas).
 // Each unordered antenna pair is drained once, by the row whose cyclic
 // distance to the other is below na / 2 (ties: the smaller index), so every
 // row drains about na / 2 columns and the warps share the work evenly: row a
@@ -507,21 +533,24 @@ __device__ __forceinline__ void fold_scalar(float* hi, float* lo, float x) {
 // col) * 2 + re/im) split into a per-lane part and a part in b and j:
 //   b >= a:  ku + 8 b + 2 j,  ku = 8 (a na - a (a - 1) / 2 - a) + 4 i + h
 //   b <  a:  8 R_b + kl + 4 j,  kl = 8 a + 2 i + h,  R_b = b na - b (b - 1) / 2 - b
-__device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, float* sVlof) {
+__device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, __nv_bfloat16* sVlof) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int q = warp & 3, h = warp >> 2;
+  const int q = warp & 3, jw = warp >> 2;  // lane quarter, and the warp's index among its 3 warps
   const int r = 32 * q + lane, a = r >> 1, i = r & 1;
   const int na = A.na;
   const bool row_ok = a < na;
   const int dmax = (na - 1) / 2 + ((na % 2 == 0 && a < na / 2) ? 1 : 0);
   const int up_hi = row_ok ? min(a + dmax, na - 1) : -1;
   const int wrap_end = row_ok ? a + dmax - na : -1;
-  const int ku = 8 * (a * na - (a * (a - 1)) / 2 - a) + 4 * i + h;
-  const int kl = 8 * a + 2 * i + h;
-  const float sgn = h ? -1.f : 1.f;
-  const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(h * 128);
+  const int ku0 = 8 * (a * na - (a * (a - 1)) / 2 - a) + 4 * i;
+  const int kl0 = 8 * a + 2 * i;
+  // 8 tasks (matrix h, column block blk) per lane quarter, dealt to its warps
 #pragma unroll 1
-  for (int blk = 0; blk < 4; ++blk) {
+  for (int task = jw; task < 8; task += 3) {
+    const int h = task >> 2, blk = task & 3;
+    const int ku = ku0 + h, kl = kl0 + h;
+    const float sgn = h ? -1.f : 1.f;
+    const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(h * 128);
     const int b_lo = 16 * blk;
     const bool need = (max(a, b_lo) <= min(up_hi, b_lo + 15)) || (wrap_end >= b_lo);
     if (!__any_sync(0xffffffffu, need)) continue;  // warp-uniform: the loads are collective
@@ -608,13 +637,17 @@ __device__ __forceinline__ SrcInfo<float> point_source_stokes(const FusedArgs<fl
 
 template <int MODE>
 __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float> A, SmemPlan S, TcPlan P) {
-  using L = StageLayout<MODE, kTcRowBytes>;
-  constexpr int KAPPA = L::kKT / 4;  // sources per stage
+  constexpr int kRowBytes = TcGeom<MODE>::kRowBytes;
+  constexpr int KAPPA = TcGeom<MODE>::kSlots;  // source slots per stage
+  constexpr int NSRC = kTcProducerWarps;       // sources per stage
+  using L = StageLayout<MODE, kRowBytes>;
+  static_assert(L::kKT == 4 * KAPPA, "stage rows hold Re and Im of every slot");
   extern __shared__ __align__(16) unsigned char smem[];
   AntInfo<float>* sa = reinterpret_cast<AntInfo<float>*>(smem + S.off_ant);
   SrcInfo<float>* ss = reinterpret_cast<SrcInfo<float>*>(smem + S.off_src);
   Jones<float>* sV = reinterpret_cast<Jones<float>*>(smem + S.off_V);
-  Jones<float>* sVlo = reinterpret_cast<Jones<float>*>(smem + S.off_Vlo);
+  __nv_bfloat16* sVlo16 = reinterpret_cast<__nv_bfloat16*>(smem + P.off_vlo16);  // tensor-core phase
+  Jones<float>* sVlo = reinterpret_cast<Jones<float>*>(smem + P.off_vlo32);      // extended sources
   int* items = reinterpret_cast<int*>(smem + S.off_items);
   double* red = reinterpret_cast<double*>(smem + S.off_red);
   unsigned char* stage = smem + P.off_stage;
@@ -622,8 +655,8 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + P.off_bar);
   uint64_t* full = bars;                    // [kTcStages], producers -> MMA
   uint64_t* empty = bars + kTcStages;       // [kTcStages], MMA commit -> producers
-  uint64_t* accfull = bars + 2 * kTcStages;  // MMA commit -> producers (drain)
-  uint64_t* accfree = accfull + 1;           // producers -> MMA
+  uint64_t* accfull = bars + 2 * kTcStages;  // MMA commit -> drain
+  uint64_t* accfree = accfull + 1;           // drain (all threads) -> MMA
   uint64_t* done = accfull + 2;              // last MMA commit
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
@@ -639,10 +672,11 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   }
   __syncthreads();
   load_antennas(A, t, ch, sa);
-  for (int i = tid; i < S.npairs; i += blockDim.x) {
-    sV[i] = jzero<float>();
-    sVlo[i] = jzero<float>();
-  }
+  for (int i = tid; i < S.npairs; i += blockDim.x) sV[i] = jzero<float>();
+  for (int i = tid; i < S.npairs * 8; i += blockDim.x) sVlo16[i] = __float2bfloat16_rn(0.f);
+  // the stage buffers' unused slots are read by the MMAs as zeros
+  for (int i = tid; i < int(kTcStages * 2 * L::kMatBytes / 16); i += blockDim.x)
+    reinterpret_cast<uint4*>(stage)[i] = make_uint4(0u, 0u, 0u, 0u);
   if (tid == 0) {
     const int npt = (A.na + 1) / 2, nqt = (A.na + 3) / 4;
     int k = 0;
@@ -653,10 +687,11 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
       tc::mbar_init(empty + i, 1);
     }
     tc::mbar_init(accfull, 1);
-    tc::mbar_init(accfree, kTcProducers);
+    tc::mbar_init(accfree, kTcThreads);
     tc::mbar_init(done, 1);
   }
-  if (warp == 8) tc::tmem_alloc(tmem_slot, kTcCols);
+  tc::fence_proxy_async_smem();
+  if (warp == kTcProducerWarps) tc::tmem_alloc(tmem_slot, kTcCols);
   tc::fence_before_thread_sync();
   __syncthreads();
   tc::fence_after_thread_sync();
@@ -665,22 +700,20 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   const float f = A.freq[ch];
   const double nu_over_c = double(f) / kLightSpeed;
   const ChanPos<float> cp = chan_pos<float>(f, A.lfreq, A.ufreq, A.nud);
-  const int nstages = (A.npsrc + KAPPA - 1) / KAPPA;
+  const int nstages = (A.npsrc + NSRC - 1) / NSRC;
   const int group = P.group;
   const float log2_ratio = log2f(f / A.ref_freq[ch]);
+  bool bad = false;
 
-  if (warp < 8) {
+  if (warp < kTcProducerWarps) {
     // ---- producers -------------------------------------------------------
-    // No barrier joins the producer warps inside the loop: every wait is a
-    // bounded mbarrier wait, and each warp drains its own TMEM lanes into
-    // pair accumulator entries no other thread touches.
-    // Item mapping: warp w covers antennas 8w .. 8w+7 and the stage's
-    // sources; lane bits 0-1 and 2 pick the antenna, bits 3-4 the source.
-    // Rows are written starting from row i0 = antenna bit 2, so that one
-    // store instruction of a warp touches all 8 rows of a core matrix and
-    // both halves of a 16-byte chunk (at most 2-way bank conflicts).
-    bool bad = false;
-    const int a = 8 * warp + (lane & 3) + 4 * ((lane >> 2) & 1);
+    // No barrier joins the warps inside the loop: every wait is a bounded
+    // mbarrier wait, and each warp drains TMEM into pair accumulator entries
+    // no other thread touches.  Warp w fills source slot w of every stage,
+    // lane l antennas l and l + 32; rows are written starting from row
+    // i0 = lane bit 2, so that 8 lanes of a store cover the 8 rows of a core
+    // matrix.
+    const int sl = warp;
     const int i0 = (lane >> 2) & 1;
     // A producer whose wait gave up (bad) skips all further waits and work;
     // the MMA warp's waits then give up too, and everyone reaches the end.
@@ -688,12 +721,12 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
       const int slot = g % kTcStages, use = g / kTcStages;
       if (!bad) bad = !tc::mbar_wait(empty + slot, (use & 1) ^ 1);
       if (!bad) {
-        const int s0 = g * KAPPA, ns = min(KAPPA, A.npsrc - s0);
+        const int s0 = g * NSRC, ns = min(NSRC, A.npsrc - s0);
         unsigned char* hi = stage + size_t(slot) * 2 * L::kMatBytes;
         unsigned char* lo = hi + L::kMatBytes;
 #pragma unroll
-        for (int rep = 0; rep < KAPPA / 4; ++rep) {
-          const int sl = (lane >> 3) + 4 * rep;
+        for (int rep = 0; rep < 2; ++rep) {
+          const int a = lane + 32 * rep;
           Jones<float> J = jzero<float>();
           if (a < A.na && sl < ns) {
             const SrcInfo<float> src = point_source_info(A, t, ch, s0 + sl, log2_ratio);
@@ -714,70 +747,93 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
         if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1);
         tc::fence_after_thread_sync();
         bad = __any_sync(0xffffffffu, bad);  // the drain's TMEM loads are warp-collective
-        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), reinterpret_cast<float*>(sVlo));
+        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), sVlo16);
         tc::fence_before_thread_sync();
         if (!bad) tc::mbar_arrive(accfree);
       }
     }
-    if (bad) *abort_flag = 1;
-  } else if (lane == 0) {
-    // ---- MMA issue ---------------------------------------------------------
+  } else {
+    // ---- MMA issue (lane 0); the whole warp drains with the producers ------
     const uint32_t idesc = L::instr(128, 128);
     const uint32_t idesc_neg = idesc | (1u << 13);  // negate A
     const int half = L::kKSteps / 2;
     bool issued = false;
-    for (int g = 0; g < nstages && !*abort_flag; ++g) {
+    for (int g = 0; g < nstages; ++g) {
       const int slot = g % kTcStages, use = g / kTcStages;
-      const bool first = (g % group) == 0;
-      if (first && g > 0) {
-        if (!tc::mbar_wait(accfree, ((g / group) - 1) & 1)) { *abort_flag = 1; break; }
+      const bool first = (g % group) == 0, last = (g % group) == group - 1 || g == nstages - 1;
+      if (lane == 0 && !bad) {
+        if (first && g > 0) {
+          bad = !tc::mbar_wait(accfree, ((g / group) - 1) & 1);
+          tc::fence_after_thread_sync();
+        }
+        if (!bad) bad = !tc::mbar_wait(full + slot, use & 1);
+        if (!bad) {
+          tc::fence_after_thread_sync();
+          const uint32_t hi = tc::smem_addr(stage + size_t(slot) * 2 * L::kMatBytes);
+          const uint32_t lo = hi + L::kMatBytes;
+          const uint32_t acc0 = (first ? 0u : 1u);
+#pragma unroll
+          for (int kk = 0; kk < L::kKSteps; ++kk) {
+            const uint32_t o = kk * L::kKStepBytes;
+            const uint64_t ah = L::desc(hi + o), al = L::desc(lo + o);
+            const uint32_t acc = kk == 0 ? acc0 : 1u;
+            L::mma(tmem, ah, ah, idesc, acc);
+            L::mma(tmem + 256, ah, al, idesc, acc);
+            L::mma(tmem + 256, al, ah, idesc, 1u);
+          }
+#pragma unroll
+          for (int kk = 0; kk < half; ++kk) {
+            const uint32_t oi = (kk + half) * L::kKStepBytes, orr = kk * L::kKStepBytes;
+            const uint64_t ih = L::desc(hi + oi), il = L::desc(lo + oi);
+            const uint64_t rh = L::desc(hi + orr), rl = L::desc(lo + orr);
+            const uint32_t acc = kk == 0 ? acc0 : 1u;
+            // D_im += A_im A_re^T
+            L::mma(tmem + 128, ih, rh, idesc, acc);
+            L::mma(tmem + 384, ih, rl, idesc, acc);
+            L::mma(tmem + 384, il, rh, idesc, 1u);
+            // D_im += (-A_re) A_im^T
+            L::mma(tmem + 128, rh, ih, idesc_neg, 1u);
+            L::mma(tmem + 384, rh, il, idesc_neg, 1u);
+            L::mma(tmem + 384, rl, ih, idesc_neg, 1u);
+          }
+          issued = true;
+          tc::mma_commit(empty + slot);
+          if (last) tc::mma_commit(accfull);
+        }
+      }
+      if (last) {
+        if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1);
         tc::fence_after_thread_sync();
+        bad = __any_sync(0xffffffffu, bad);
+        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), sVlo16);
+        tc::fence_before_thread_sync();
+        if (!bad) tc::mbar_arrive(accfree);
       }
-      if (!tc::mbar_wait(full + slot, use & 1)) { *abort_flag = 1; break; }
-      tc::fence_after_thread_sync();
-      const uint32_t hi = tc::smem_addr(stage + size_t(slot) * 2 * L::kMatBytes);
-      const uint32_t lo = hi + L::kMatBytes;
-      const uint32_t acc0 = (first ? 0u : 1u);
-#pragma unroll
-      for (int kk = 0; kk < L::kKSteps; ++kk) {
-        const uint32_t o = kk * L::kKStepBytes;
-        const uint64_t ah = L::desc(hi + o), al = L::desc(lo + o);
-        const uint32_t acc = kk == 0 ? acc0 : 1u;
-        L::mma(tmem, ah, ah, idesc, acc);
-        L::mma(tmem + 256, ah, al, idesc, acc);
-        L::mma(tmem + 256, al, ah, idesc, 1u);
-      }
-#pragma unroll
-      for (int kk = 0; kk < half; ++kk) {
-        const uint32_t oi = (kk + half) * L::kKStepBytes, orr = kk * L::kKStepBytes;
-        const uint64_t ih = L::desc(hi + oi), il = L::desc(lo + oi);
-        const uint64_t rh = L::desc(hi + orr), rl = L::desc(lo + orr);
-        const uint32_t acc = kk == 0 ? acc0 : 1u;
-        // D_im += A_im A_re^T
-        L::mma(tmem + 128, ih, rh, idesc, acc);
-        L::mma(tmem + 384, ih, rl, idesc, acc);
-        L::mma(tmem + 384, il, rh, idesc, 1u);
-        // D_im += (-A_re) A_im^T
-        L::mma(tmem + 128, rh, ih, idesc_neg, 1u);
-        L::mma(tmem + 384, rh, il, idesc_neg, 1u);
-        L::mma(tmem + 384, rl, ih, idesc_neg, 1u);
-      }
-      issued = true;
-      tc::mma_commit(empty + slot);
-      if ((g % group) == group - 1 || g == nstages - 1) tc::mma_commit(accfull);
     }
-    if (issued) {  // all MMAs finished before TMEM is released
+    if (lane == 0 && issued) {  // all MMAs finished before TMEM is released
       tc::mma_commit(done);
-      if (!tc::mbar_wait(done, 0)) *abort_flag = 1;
+      if (!tc::mbar_wait(done, 0)) bad = true;
     }
   }
+  if (bad) *abort_flag = 1;
   tc::fence_before_thread_sync();
   __syncthreads();
   tc::fence_after_thread_sync();
-  if (warp == 8) tc::tmem_dealloc(tmem, kTcCols);
+  if (warp == kTcProducerWarps) tc::tmem_dealloc(tmem, kTcCols);
   const bool aborted = *abort_flag != 0;
 
   // ---- extended sources on the CUDA cores --------------------------------
+  // the tensor-core phase's BF16 low parts join the high parts; the
+  // extended sources accumulate with FP32 low parts in the stage region
+  {
+    float* v = reinterpret_cast<float*>(sV);
+    float* vlo = reinterpret_cast<float*>(sVlo);
+    for (int i = tid; i < S.npairs * 8; i += blockDim.x) {
+      v[i] += __bfloat162float(sVlo16[i]);
+      vlo[i] = 0.f;
+    }
+  }
+  __syncthreads();
   const float kg = A.gauss_scale * f, ks = A.two_pi_over_c * f;
   for (int s0 = A.npsrc; s0 < A.nsrc && !aborted;) {
     const int s1 = min(s0 + S.st, A.nsrc), ns = s1 - s0;
@@ -1957,17 +2013,29 @@ mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2,
   S.groups = S.nitems <= kTcThreads ? std::min(8, std::max(1, kTcThreads / S.nitems)) : 1;
   TcPlan P;
   P.group = kTcGroup;
-  // Stage buffers first (128-byte aligned), then the CUDA-core plan's regions,
-  // shifted; the extended-source Jones tile reuses the stage buffers.
-  const size_t stage_bytes = size_t(kTcStages) * 2 * StageGeometry<kTcRowBytes>::kMatBytes;
-  const size_t need_J = sizeof(Jones<float>) * S.st * S.nap;
-  const size_t stage_region = align_up(std::max(stage_bytes, need_J), 128);
-  P.off_stage = 0;
-  S.off_ant += stage_region; S.off_src += stage_region; S.off_V += stage_region;
-  S.off_Vlo += stage_region; S.off_items += stage_region; S.off_red += stage_region;
-  S.off_J = 0;
-  P.off_bar = align_up(S.total + stage_region, 16);
-  P.total = P.off_bar + (2 * kTcStages + 3) * sizeof(uint64_t) + 16;
+  // The stage region holds the operand stages during the tensor-core phase,
+  // then the extended sources' Jones tile and the FP32 low parts of the pair
+  // accumulators; the BF16 low parts of the tensor-core phase have their own
+  // region.  All regions 128-byte aligned.
+  const size_t row_bytes = mode == MB_MODE_SPLIT_TF32 ? TcGeom<MB_MODE_SPLIT_TF32>::kRowBytes
+                                                      : TcGeom<MB_MODE_SPLIT_BF16>::kRowBytes;
+  const size_t stage_bytes = size_t(kTcStages) * 2 * 128 * row_bytes;
+  const size_t jbytes = align_up(sizeof(Jones<float>) * S.st * S.nap, 128);
+  const size_t vbytes = sizeof(Jones<float>) * S.npairs;
+  size_t o = 0;
+  auto take = [&o](size_t b) { size_t r = o; o = align_up(o + b, 128); return r; };
+  P.off_stage = take(std::max(stage_bytes, jbytes + vbytes));
+  P.off_vlo32 = P.off_stage + jbytes;
+  S.off_J = P.off_stage;
+  S.off_Vlo = P.off_vlo32;
+  S.off_ant = take(sizeof(AntInfo<float>) * A.na);
+  S.off_src = take(sizeof(SrcInfo<float>) * S.st);
+  S.off_V = take(vbytes);
+  P.off_vlo16 = take(size_t(S.npairs) * 8 * sizeof(__nv_bfloat16));
+  S.off_items = take(sizeof(int) * (S.nitems + 128));
+  S.off_red = take(sizeof(double) * 32);
+  P.off_bar = take((2 * kTcStages + 3) * sizeof(uint64_t) + 16);
+  P.total = o;
   if (P.total > 227 * 1024)
     return fail(MB_ERR_UNSUPPORTED, "split-precision kernel needs %zu bytes of shared memory for na=%d",
                 P.total, A.na);
