@@ -1357,9 +1357,9 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
 // Then, with gJ = dJ,
 //   d sqrt(B) = EK^H gJ,  d/dl_beam = Re tr(gJ^H Pl),  d/dm_beam = Re tr(gJ^H Pm),
 //   d/dphi = 2 pi nu / c * Im tr(d sqrt(B)^H sqrt(B)).
-// Lane 0 of each group's first warp issues the group's MMAs once the group
-// has staged its tile (group barrier); while one group waits for its MMAs
-// the other computes.
+// Lane 0 of the group's first and second warps issue the Re and Im MMA
+// chains once the group has staged its tile (group barrier); while one group
+// waits for its MMAs the others compute.
 constexpr int kTaRowBytes = 512;      // 256 BF16 values of K per operand row
 constexpr int kTaKappa = 8;           // sources per tile (16 operand rows)
 constexpr int kTaGroups = 3;          // worker groups = stages = TMEM regions
@@ -1466,37 +1466,35 @@ struct TaPlan {
   size_t off_park, off_stage, off_ant, off_acc, off_bar, total;
 };
 
-// The MMAs of one tile: dJ = Y J from the Y operand in TMEM (ytm: column 0,
-// lane 0) and the tile's J operand at jsm (shared-memory address of the hi
-// part; the lo part follows, and J's lo rows sit where rows 16-31 of a 32-row
-// operand would, so one N = 32 MMA forms Y_hi [J_hi; J_lo]^T).  Per K step
-// (16 values: 8 TMEM columns of Y) and chain:
+// The MMAs of one tile for one chain of dJ = Y J, from the Y operand in
+// TMEM (ytm: column 0, lane 0) and the tile's J operand at jsm (shared-memory
+// address of the hi part; the lo part follows, and J's lo rows sit where
+// rows 16-31 of a 32-row operand would, so one N = 32 MMA forms
+// Y_hi [J_hi; J_lo]^T).  Per K step (16 values: 8 TMEM columns of Y):
 //   D[0:16] += Y_hi J_hi^T,  D[16:32] += Y_hi J_lo^T   (N = 32)
 //   D[0:16] += Y_lo J_hi^T                             (N = 16)
-// Chain Re at d + 0 (all K steps), chain Im at d + 32 (-Y_im Re J, then
-// Y_re Im J, negate-A bit for the first); dJ = D[0:16] + D[16:32] of each.
-__device__ __forceinline__ void ta_issue_mma(uint32_t d, uint32_t ytm, uint32_t jsm) {
+// Chain Re (im = false) accumulates at d over all K steps; chain Im (im =
+// true) at d as -Y_im Re J (negate-A bit) plus Y_re Im J.  dJ = D[0:16] +
+// D[16:32].  The two chains go to different accumulators and are issued by
+// different threads, in parallel.
+__device__ __forceinline__ void ta_issue_chain(bool im, uint32_t d, uint32_t ytm, uint32_t jsm) {
   constexpr uint32_t id32 = TaLayout::instr(128, 32), id16 = TaLayout::instr(128, 16);
-  constexpr uint32_t neg = 1u << 13;  // negate A
+  const uint32_t neg = im ? (1u << 13) : 0u;  // negate A for -Y_im
   const uint32_t yh = ytm, yl = ytm + 128;
   const uint64_t jh = TaGeom::desc(jsm);
   constexpr uint64_t kStep = TaGeom::kKStepBytes >> 4;
   constexpr int half = TaGeom::kKSteps / 2;
-  const uint32_t dre = d, dim = d + 32;
 #pragma unroll
   for (int kk = 0; kk < half; ++kk) {
     const uint64_t ore = kk * kStep, oim = (kk + half) * kStep;  // J descriptor steps
     const uint32_t cre = 8 * kk, cim = 8 * (kk + half);          // Y columns
     const uint32_t acc = kk == 0 ? 0u : 1u;
-    // Re: K steps of Re J (ore) and of Im J (oim)
-    tc::mma_f16_ta(dre, yh + cre, jh + ore, id32, acc);
-    tc::mma_f16_ta(dim, yh + cim, jh + ore, id32 | neg, acc);
-    tc::mma_f16_ta(dre, yl + cre, jh + ore, id16, 1u);
-    tc::mma_f16_ta(dim, yl + cim, jh + ore, id16 | neg, 1u);
-    tc::mma_f16_ta(dre, yh + cim, jh + oim, id32, 1u);
-    tc::mma_f16_ta(dim, yh + cre, jh + oim, id32, 1u);
-    tc::mma_f16_ta(dre, yl + cim, jh + oim, id16, 1u);
-    tc::mma_f16_ta(dim, yl + cre, jh + oim, id16, 1u);
+    // Re: Y_re Re J + (-Y_im) Im J;  Im: (-Y_im) Re J (negated: Y_im Re J) + Y_re Im J
+    const uint32_t c1 = im ? cim : cre, c2 = im ? cre : cim;
+    tc::mma_f16_ta(d, yh + c1, jh + ore, id32 | neg, acc);
+    tc::mma_f16_ta(d, yl + c1, jh + ore, id16 | neg, 1u);
+    tc::mma_f16_ta(d, yh + c2, jh + oim, id32, 1u);
+    tc::mma_f16_ta(d, yl + c2, jh + oim, id16, 1u);
   }
 }
 
@@ -1524,8 +1522,8 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
   for (int i = tid; i < kTaGroups * 2 * kTaKappa * kTaAcc; i += blockDim.x) sacc[i] = 0.f;
   if (tid == 0) {
     for (int g = 0; g < kTaGroups; ++g) {
-      tc::mbar_init(dfull + g, 1);
-      tc::mbar_init(done + g, 1);
+      tc::mbar_init(dfull + g, 2);  // one commit per chain issuer
+      tc::mbar_init(done + g, 2);
     }
   }
   tc::fence_proxy_async_smem();
@@ -1570,7 +1568,7 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
 
   {
     const int grp = warp >> 2, q = warp & 3;
-    const bool issuer = q == 0 && lane == 0;
+    const bool issuer = q < 2 && lane == 0;  // warp q = 0 issues chain Re, q = 1 chain Im
     bool issued = false;
     const int r = 32 * q + lane, a = r >> 1, i = r & 1;
     const bool ant_ok = a < A.na;
@@ -1640,7 +1638,8 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
       if (group_sync_or(grp, bad)) { bad = true; break; }
       if (issuer) {
         tc::fence_after_thread_sync();
-        ta_issue_mma(tmem + kTaYCols + uint32_t(kTaGroupCols * grp), tmem, tc::smem_addr(hi));
+        ta_issue_chain(q == 1, tmem + kTaYCols + uint32_t(kTaGroupCols * grp) + uint32_t(32 * q), tmem,
+                       tc::smem_addr(hi));
         tc::mma_commit(dfull + grp);
         issued = true;
       }
