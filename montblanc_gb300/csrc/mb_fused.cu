@@ -979,13 +979,43 @@ __device__ void beam_interp_d(const T* __restrict__ E_beam, const BeamGeom& G, c
   }
 }
 
-// Same as beam_interp_d on the frequency-blended plane (4 corners).
+// Same as beam_interp_d on the frequency-blended plane (4 corners).  In
+// FP32 each of the 12 plane values is interpolated in the difference form
+//   f = f00 + x (f10 - f00) + y (b + x c),  b = f01 - f00,
+//   c = f11 - f10 - b,  df/dx = (f10 - f00) + y c,  df/dy = b + x c,
+// the same bilinear function and derivatives with fewer operations.
 template <typename T>
 __device__ void beam_interp_plane_d(const T* __restrict__ plane, int mh, const GridPos<T>& gl, const GridPos<T>& gm,
                                     Jones<T>& E, Jones<T>& dEl, Jones<T>& dEm) {
   Jones<T> sum = jzero<T>(), dsl = jzero<T>(), dsm = jzero<T>();
   T amp[4] = {0, 0, 0, 0}, dal[4] = {0, 0, 0, 0}, dam[4] = {0, 0, 0, 0};
   const T ld = gl.d, md = gm.d;
+  if constexpr (sizeof(T) == 4) {
+    const float4* p00 = reinterpret_cast<const float4*>(plane + kPlaneVals * (size_t(gl.i0) * mh + gm.i0));
+    const float4* p10 = reinterpret_cast<const float4*>(plane + kPlaneVals * (size_t(gl.i1) * mh + gm.i0));
+    const float4* p01 = reinterpret_cast<const float4*>(plane + kPlaneVals * (size_t(gl.i0) * mh + gm.i1));
+    const float4* p11 = reinterpret_cast<const float4*>(plane + kPlaneVals * (size_t(gl.i1) * mh + gm.i1));
+    float* sv = reinterpret_cast<float*>(&sum);
+    float* lv = reinterpret_cast<float*>(&dsl);
+    float* mv = reinterpret_cast<float*>(&dsm);
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {  // float4 runs: E.a E.b | E.c E.d | |E|
+      const float4 q00 = __ldg(p00 + v), q10 = __ldg(p10 + v), q01 = __ldg(p01 + v), q11 = __ldg(p11 + v);
+      const float f00[4] = {q00.x, q00.y, q00.z, q00.w}, f10[4] = {q10.x, q10.y, q10.z, q10.w};
+      const float f01[4] = {q01.x, q01.y, q01.z, q01.w}, f11[4] = {q11.x, q11.y, q11.z, q11.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float a = f10[k] - f00[k], b = f01[k] - f00[k], c = f11[k] - f10[k] - b;
+        const float fy = fmaf(ld, c, b), fx = fmaf(md, c, a);
+        const float fv = fmaf(md, fy, fmaf(ld, a, f00[k]));
+        if (v < 2) {
+          sv[4 * v + k] = fv; lv[4 * v + k] = fx; mv[4 * v + k] = fy;
+        } else {
+          amp[k] = fv; dal[k] = fx; dam[k] = fy;
+        }
+      }
+    }
+  } else {
 #pragma unroll
   for (int corner = 0; corner < 4; ++corner) {
     const bool hl = corner & 1, hm = corner & 2;
@@ -1011,6 +1041,7 @@ __device__ void beam_interp_plane_d(const T* __restrict__ plane, int mh, const G
       l4[k] = l4[k] + e4[k] * wl; dal[k] += wl * ab;
       m4[k] = m4[k] + e4[k] * wm; dam[k] += wm * ab;
     }
+  }
   }
   Cx<T>* E4 = &E.a; Cx<T>* dl4 = &dEl.a; Cx<T>* dm4 = &dEm.a;
   const Cx<T>* s4 = &sum.a; const Cx<T>* l4 = &dsl.a; const Cx<T>* m4 = &dsm.a;
