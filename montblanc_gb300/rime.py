@@ -192,3 +192,89 @@ def rime_chi2(problem, lm, stokes, alpha, gauss_shape, sersic_shape, G_term, mod
     convention for real-valued losses.  K and E are recomputed in the
     backward pass rather than stored."""
     return _RimeChi2.apply(problem, mode, lm, stokes, alpha, gauss_shape, sersic_shape, G_term)
+
+
+class HostFeed(object):
+    """chi^2 and gradient of a sequence of input sets that live in host
+    memory, with the transfers overlapped with the kernels.
+
+    Each ``submit`` copies one set of host arrays (``names``: any of the
+    problem's input arrays, e.g. observed_vis, flag, G_term and the source
+    parameters) to the device on a host-to-device stream, runs the fused
+    forward and adjoint on a compute stream once that copy has landed, and
+    copies chi^2 and the gradients back into the caller's host tensors on a
+    device-to-host stream.  ``depth`` sets of device buffers rotate, so the
+    copies of set i+1 and the read-back of set i-1 run while the kernels of
+    set i do.  Host tensors should be pinned for the copies to be
+    asynchronous; a submitted set's host inputs and outputs must stay alive
+    and untouched until its ``done`` event has completed."""
+
+    def __init__(self, problem, names, mode='native', depth=2, grad_scale=1.0):
+        for n in names:
+            if n not in _cabi.INPUT_NAMES or problem.arrays.get(n) is None:
+                raise ValueError('%s is not an input array of this problem' % n)
+        if depth < 1:
+            raise ValueError('depth must be at least 1')
+        self.problem, self.mode, self.names = problem, mode, tuple(names)
+        self.grad_scale = float(grad_scale)
+        dev = problem.device
+        self.h2d = torch.cuda.Stream(dev)
+        self.compute = torch.cuda.Stream(dev)
+        self.d2h = torch.cuda.Stream(dev)
+        self.slots = []
+        for _ in range(depth):
+            self.slots.append({
+                'inputs': {n: torch.empty_like(problem.arrays[n]) for n in self.names},
+                'grads': problem.empty_grads(),
+                'x2': torch.zeros(1, dtype=torch.float64, device=dev),
+                'loaded': torch.cuda.Event(enable_timing=True),
+                'computed': torch.cuda.Event(enable_timing=True),
+                'done': torch.cuda.Event(enable_timing=True),
+                'used': False,
+            })
+        self.count = 0
+
+    def submit(self, host_inputs, x2_out, grads_out, events=None):
+        """Queue one set: ``host_inputs`` {name: host tensor} for every name
+        of the feed, ``x2_out`` a 1-element float64 host tensor and
+        ``grads_out`` {name: host tensor} (any subset of the gradient names)
+        receiving the results.  Returns the event recorded after the
+        read-back.  ``events``, if given, is a list of four timing events
+        recorded before and after the copy in, after the kernels and after
+        the read-back."""
+        s = self.slots[self.count % len(self.slots)]
+        self.count += 1
+        p = self.problem
+        with torch.cuda.stream(self.h2d):
+            if s['used']:
+                self.h2d.wait_event(s['computed'])   # the previous set's kernels read these buffers
+            if events:
+                events[0].record(self.h2d)
+            for n in self.names:
+                s['inputs'][n].copy_(host_inputs[n], non_blocking=True)
+            s['loaded'].record(self.h2d)
+            if events:
+                events[1].record(self.h2d)
+        self.compute.wait_event(s['loaded'])
+        if s['used']:
+            self.compute.wait_event(s['done'])       # the previous set's gradients have been read back
+        x2 = p.forward(mode=self.mode, want_grad=True, X2=s['x2'], stream=self.compute, overrides=s['inputs'])
+        p.adjoint(mode=self.mode, grad_scale=self.grad_scale, grads=s['grads'], stream=self.compute,
+                  overrides=s['inputs'])
+        s['computed'].record(self.compute)
+        if events:
+            events[2].record(self.compute)
+        with torch.cuda.stream(self.d2h):
+            self.d2h.wait_event(s['computed'])
+            x2_out.copy_(x2, non_blocking=True)
+            for n, t in grads_out.items():
+                t.copy_(s['grads'][n], non_blocking=True)
+            s['done'].record(self.d2h)
+            if events:
+                events[3].record(self.d2h)
+        s['used'] = True
+        return s['done']
+
+    def synchronize(self):
+        for st in (self.h2d, self.compute, self.d2h):
+            st.synchronize()
