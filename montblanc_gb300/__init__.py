@@ -42,8 +42,8 @@ def sources(**kwargs):
 
 def rime_solver_cfg(**kwargs):
     """Solver configuration dict (montblanc/__init__.py:96-126).  Unlike the
-    reference the data source defaults to 'default' since no MeasurementSet
-    loader is part of this package."""
+    reference the data source defaults to 'default': a MeasurementSet is read
+    only when data_source='ms' and msfile are given."""
     cfg = gen_cfg(**kwargs)
     cfg.setdefault(Options.DATA_SOURCE, Options.DATA_SOURCE_DEFAULT)
     return cfg
@@ -56,14 +56,31 @@ def rime_solver(slvr_cfg):
     version = slvr_cfg.get(Options.VERSION, Options.DEFAULT_VERSION)
     if version not in (Options.VERSION_FOUR, Options.VERSION_FIVE):
         raise ValueError('Invalid version %s (this package implements the v4 path)' % version)
-    if slvr_cfg.get(Options.DATA_SOURCE) == Options.DATA_SOURCE_MS:
-        raise NotImplementedError('MeasurementSet loading is not part of montblanc_gb300; '
-                                  "use data_source='default', 'test' or 'empty' and transfer arrays")
     if version == Options.VERSION_FIVE:
-        from .composite import CompositeRimeSolver
-        return CompositeRimeSolver(slvr_cfg)
-    from .solver import RimeSolver
-    return RimeSolver(slvr_cfg)
+        from .composite import CompositeRimeSolver as cls
+    else:
+        from .solver import RimeSolver as cls
+    if slvr_cfg.get(Options.DATA_SOURCE) == Options.DATA_SOURCE_MS:
+        return rime_solver_from_ms(cls, slvr_cfg)
+    return cls(slvr_cfg)
+
+
+def rime_solver_from_ms(cls, slvr_cfg):
+    """A solver of class ``cls`` sized by, and holding the arrays of, the
+    MeasurementSet ``slvr_cfg['msfile']`` (montblanc/factory.py:113-148)."""
+    from .ms import MeasurementSetLoader
+    if Options.MS_FILE not in slvr_cfg:
+        raise KeyError("%s is '%s' in the solver configuration, but no MeasurementSet is given in the %s key"
+                       % (Options.DATA_SOURCE, Options.DATA_SOURCE_MS, Options.MS_FILE))
+    cfg = dict(slvr_cfg)
+    with MeasurementSetLoader(cfg[Options.MS_FILE], auto_correlations=cfg.get(Options.AUTO_CORRELATIONS,
+                                                                              False)) as loader:
+        ntime, nbl, na, nbands, nchan = loader.get_dims()
+        cfg.update({Options.NTIME: ntime, Options.NA: na, Options.NBL: nbl, Options.NBANDS: nbands,
+                    Options.NCHAN: nchan})
+        slvr = cls(cfg)
+        loader.load(slvr, cfg)
+        return slvr
 
 
 def __getattr__(name):

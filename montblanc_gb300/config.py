@@ -3,8 +3,9 @@
 The option names, defaults and valid values are the reference's
 (``montblanc/slvr_config.py:61-255``, ``montblanc/impl/rime/slvr_config.py:35-201``)
 so that a configuration dict written for the reference configures this
-solver the same way.  Only the keys that matter to the RIME v4 path are
-interpreted; MeasurementSet and multi-solver keys are accepted and ignored.
+solver the same way.  Only the keys that matter to the RIME v4 path, the
+streaming (v5) driver and MeasurementSet input are interpreted; others are
+accepted and ignored.
 
 ``ARRAYS`` and ``PROPERTIES`` restate the v4 array/property table of
 ``montblanc/impl/rime/v4/config.py:54-69, 131-247``: names, symbolic shapes,
@@ -37,6 +38,10 @@ class Options:
     DATA_SOURCE_EMPTY = 'empty'
     MS_FILE = 'msfile'
     CONTEXT = 'context'
+    INIT_WEIGHTS = 'init_weights'
+    INIT_WEIGHTS_NONE = None
+    INIT_WEIGHTS_SIGMA = 'sigma'
+    INIT_WEIGHTS_WEIGHT = 'weight'
     # montblanc/impl/rime/slvr_config.py
     E_BEAM_WIDTH = 'beam_lw'
     E_BEAM_HEIGHT = 'beam_mh'
@@ -91,6 +96,7 @@ VALID = {
     Options.RIME_MODE: ('native', 'split_tf32', 'split_bf16'),
     Options.DATA_SOURCE: (Options.DATA_SOURCE_DEFAULT, Options.DATA_SOURCE_MS, Options.DATA_SOURCE_TEST,
                           Options.DATA_SOURCE_EMPTY),
+    Options.INIT_WEIGHTS: (Options.INIT_WEIGHTS_NONE, Options.INIT_WEIGHTS_SIGMA, Options.INIT_WEIGHTS_WEIGHT),
 }
 
 
