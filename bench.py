@@ -241,7 +241,8 @@ def build_workload(name, seed):
 def batched_likelihood(seed, nsets=256, reps=2):
     """256 parameter sets (per-set source counts log-uniform in 10..5000,
     point / gaussian / sersic mix) against one 100 x 27 x 64 observation:
-    chi^2 + gradient of every set per batch, the forms autotuned per set,
+    chi^2 + gradient of every set per batch, the form and source tile
+    autotuned per set,
     the batch captured as one CUDA graph and replayed.  Errors against the
     FP64 form on the smallest, median and largest sets."""
     import numpy as np
@@ -291,7 +292,10 @@ def batched_likelihood(seed, nsets=256, reps=2):
                         '(%d sources in all), shared observation' % (nsets, int(n.sum())),
             'sets_per_s': nsets / (ms * 1e-3), 'terms_per_s': b.terms() / (ms * 1e-3), 'ms_per_batch': ms,
             'execution': 'one CUDA graph replay per batch (forward + adjoint of every set)',
-            'forms': {f: forms.count(f) for f in set(forms)}, 'autotune_s': tune_s,
+            'forms': {f: forms.count(f) for f in set(forms)},
+            'choices': {'%s/%d' % c: n_c for c, n_c in
+                        ((c, list(zip(b.forms, b.tiles)).count(c)) for c in set(zip(b.forms, b.tiles)))},
+            'autotune_s': tune_s,
             'autotune_ms_by_nsrc': b.tune_times,
             'errors_vs_fp64': {'sets': [int(n[i]) for i in pick], 'chi2_rel': x2_err, 'grad_rel_norm': g_err}}
 

@@ -56,6 +56,16 @@ typedef enum mb_mode {
 /* Option bits */
 #define MB_APPLY_WEIGHTS 0x1u /* weight chi^2 terms by weight_vector */
 #define MB_RESIDUALS 0x2u     /* write observed - model instead of model */
+/* Source tile of the CUDA-core coherency kernels (the native forms and the
+ * extended sources' adjoint of the split forms): sources per shared-memory
+ * tile, a tuning hint that does not change results beyond rounding order.
+ * 0 keeps the default (16 in FP32, 8 in FP64); a tile whose shared memory
+ * does not fit is halved until it does. */
+#define MB_SOURCE_TILE_SHIFT 8
+#define MB_SOURCE_TILE_MASK (0x3u << MB_SOURCE_TILE_SHIFT)
+#define MB_SOURCE_TILE_8 (0x1u << MB_SOURCE_TILE_SHIFT)
+#define MB_SOURCE_TILE_16 (0x2u << MB_SOURCE_TILE_SHIFT)
+#define MB_SOURCE_TILE_32 (0x3u << MB_SOURCE_TILE_SHIFT)
 
 typedef struct mb_dim {
   uint32_t global_size;

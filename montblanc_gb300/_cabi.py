@@ -28,6 +28,18 @@ MB_MODE_NATIVE, MB_MODE_SPLIT_TF32, MB_MODE_SPLIT_BF16 = 0, 1, 2
 MODES = {'native': MB_MODE_NATIVE, 'split_tf32': MB_MODE_SPLIT_TF32, 'split_bf16': MB_MODE_SPLIT_BF16}
 MB_APPLY_WEIGHTS = 0x1
 MB_RESIDUALS = 0x2
+MB_SOURCE_TILE_SHIFT = 8
+MB_SOURCE_TILE_MASK = 0x3 << MB_SOURCE_TILE_SHIFT
+SOURCE_TILES = {0: 0, 8: 0x1 << MB_SOURCE_TILE_SHIFT, 16: 0x2 << MB_SOURCE_TILE_SHIFT,
+                32: 0x3 << MB_SOURCE_TILE_SHIFT}
+
+
+def source_tile_bits(tile):
+    """Option bits asking the CUDA-core kernels for ``tile`` sources per
+    shared-memory tile (0: the library's default)."""
+    if tile not in SOURCE_TILES:
+        raise ValueError('source tile %r is not one of %s' % (tile, sorted(SOURCE_TILES)))
+    return SOURCE_TILES[tile]
 MB_TC_SELFTEST_A_IN_TMEM = 0x10
 
 DIM_NAMES = ('ntime', 'na', 'nbl', 'nchan', 'npol', 'npolchan', 'nsrc', 'npsrc', 'ngsrc', 'nssrc',

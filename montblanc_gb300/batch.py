@@ -11,10 +11,11 @@ per-set ``mb_rime_forward`` / ``mb_rime_adjoint`` sequence is captured once
 and replayed, so a batch costs one graph launch.
 
 The kernel form of each set (CUDA-core ``native`` or tensor-core
-``split_tf32``) is chosen by ``autotune``, which times both forms on
-representative sets of each source-count range and keeps the faster one:
-small source counts favour the CUDA-core tiles, large ones the tensor
-cores.
+``split_tf32``) and the source tile of its CUDA-core kernels (sources per
+shared-memory tile: 8, 16 or 32) are chosen by ``autotune``, which times
+every candidate on representative sets of each source-count range and keeps
+the fastest: small source counts favour the CUDA-core tiles, large ones the
+tensor cores.
 """
 import ctypes
 
@@ -29,6 +30,10 @@ SHARED_FLOAT = ('uvw', 'frequency', 'ref_frequency', 'parallactic_angles', 'poin
 SHARED_COMPLEX = ('E_beam', 'G_term', 'observed_vis')
 PER_SET = ('lm', 'stokes', 'alpha', 'gauss_shape', 'sersic_shape')
 FORMS = ('native', 'split_tf32')
+#: (form, source tile) pairs the autotuner times by default; tile 0 is the
+#: library default.  The tile only concerns the CUDA-core kernels: all of a
+#: native set, the extended sources' adjoint of a split set.
+CANDIDATES = (('native', 8), ('native', 16), ('native', 32), ('split_tf32', 0), ('split_tf32', 32))
 
 
 def make_sets(P, nsets, seed=0, lo=10, hi=5000, gauss_fraction=0.16, sersic_fraction=0.04):
@@ -111,6 +116,7 @@ class RimeBatch(object):
                        if want_G_grad else None)
         self.X2 = torch.zeros(self.nsets, dtype=torch.float64, device=dev)
         self.forms = ['split_tf32' if dtype == 'float' else 'native'] * self.nsets
+        self.tiles = [0] * self.nsets
         self._graph = None
         self._ws = None
 
@@ -119,8 +125,8 @@ class RimeBatch(object):
         npt, ng, ns = self.counts[i]
         return _cabi.make_dims(self.ntime, self.na, self.nbl, self.nchan, npt, ng, ns, beam=self.beam)
 
-    def _options(self):
-        o = 0
+    def _options(self, i=None):
+        o = _cabi.source_tile_bits(self.tiles[i]) if i is not None else 0
         if self.use_weight_vector:
             o |= _cabi.MB_APPLY_WEIGHTS
         if self.residuals:
@@ -173,10 +179,10 @@ class RimeBatch(object):
         props = _cabi.make_props(**self.props)
         inp = self._inputs(i)
         ws = self._ws
-        _cabi.call('mb_rime_forward', self.mb_dtype, mode, ctypes.byref(d), ctypes.byref(props), self._options(),
+        _cabi.call('mb_rime_forward', self.mb_dtype, mode, ctypes.byref(d), ctypes.byref(props), self._options(i),
                    ctypes.byref(inp), None, None, ptr(self.X2) + 8 * i, 1, ptr(ws), ws.numel(), handle)
         g = self._grad_struct(i)
-        _cabi.call('mb_rime_adjoint', self.mb_dtype, mode, ctypes.byref(d), ctypes.byref(props), self._options(),
+        _cabi.call('mb_rime_adjoint', self.mb_dtype, mode, ctypes.byref(d), ctypes.byref(props), self._options(i),
                    ctypes.byref(inp), 1.0, ctypes.byref(g), ptr(ws), ws.numel(), handle)
 
     def enqueue(self, stream=None):
@@ -185,8 +191,9 @@ class RimeBatch(object):
             self.enqueue_set(i, stream)
 
     # ---- tuning and graphs -------------------------------------------------------------
-    def _time_set(self, i, form, reps):
+    def _time_set(self, i, form, reps, tile=0):
         self.forms[i] = form
+        self.tiles[i] = tile
         self.workspace()
         self.enqueue_set(i)
         torch.cuda.synchronize(self.device)
@@ -199,15 +206,20 @@ class RimeBatch(object):
         e1.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    def autotune(self, forms=FORMS, buckets=8, reps=2):
-        """Choose the kernel form of every set by measurement.
+    def autotune(self, forms=None, buckets=8, reps=2, candidates=None):
+        """Choose the kernel form and source tile of every set by measurement.
 
         Sets are grouped into ``buckets`` ranges of log source count; the set
-        at each bucket's median is timed in every candidate form (CUDA
-        events, after one warm-up) and the bucket takes the fastest.
-        ``buckets=None`` times every set.  Returns the per-set choice."""
+        at each bucket's median is timed with every candidate (form, source
+        tile) pair (CUDA events, after one warm-up) and the bucket takes the
+        fastest.  ``forms`` restricts the candidates to those forms;
+        ``buckets=None`` times every set.  Returns the per-set forms (the
+        tiles are in ``self.tiles``)."""
+        cands = list(candidates or CANDIDATES)
+        if forms is not None:
+            cands = [c for c in cands if c[0] in forms]
         if self.dtype != 'float':
-            forms = ('native',)
+            cands = [c for c in cands if c[0] == 'native'] or [('native', 0)]
         n = np.array([sum(c) for c in self.counts])
         if buckets is None or buckets >= self.nsets:
             groups = [[i] for i in range(self.nsets)]
@@ -216,18 +228,18 @@ class RimeBatch(object):
             idx = np.clip(np.searchsorted(edges, np.log(n), side='right') - 1, 0, buckets - 1)
             groups = [list(np.nonzero(idx == b)[0]) for b in range(buckets)]
             groups = [g for g in groups if g]
-        choice = list(self.forms)
+        forms_out, tiles_out = list(self.forms), list(self.tiles)
         self.tune_times = {}
         for g in groups:
             rep_set = int(g[np.argsort(n[g])[len(g) // 2]])
-            t = [self._time_set(rep_set, f, reps) for f in forms]
-            best = forms[int(np.argmin(t))]
-            self.tune_times[int(n[rep_set])] = dict(zip(forms, t))
+            t = [self._time_set(rep_set, f, reps, tile) for f, tile in cands]
+            best = cands[int(np.argmin(t))]
+            self.tune_times[int(n[rep_set])] = {'%s/%d' % c: ms for c, ms in zip(cands, t)}
             for i in g:
-                choice[i] = best
-        self.forms = choice
+                forms_out[i], tiles_out[i] = best
+        self.forms, self.tiles = forms_out, tiles_out
         self._graph = None
-        return choice
+        return forms_out
 
     def capture(self):
         """Capture the whole batch as one CUDA graph (forms fixed)."""

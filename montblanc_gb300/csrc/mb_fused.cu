@@ -63,6 +63,8 @@ __device__ __forceinline__ T* y_full(T* sY, int a, int b, int na) { return sY + 
 // (a, d, Re b, Im b), alpha / 2, 0, l / n, m / n.
 constexpr int kBsqVals = 8;
 
+constexpr size_t kMaxDynamicSmem = 227 * 1024;  // per CTA on sm_100 / sm_103
+
 int count_pair_tiles(int na, int RP, int RQ) {
   int npt = (na + RP - 1) / RP, nqt = (na + RQ - 1) / RQ, n = 0;
   for (int ip = 0; ip < npt; ++ip) n += nqt - (ip * RP) / RQ;
@@ -70,11 +72,25 @@ int count_pair_tiles(int na, int RP, int RQ) {
 }
 
 // with_J = false leaves out the Jones tile (a caller that places it itself).
+// tile > 0 asks for that many sources per tile; the tile is halved (down to
+// 4) while the plan does not fit the shared memory of one CTA.
 template <typename T>
-SmemPlan make_plan(int na, bool adjoint, bool with_J = true) {
+SmemPlan make_plan_tile(int na, bool adjoint, bool with_J, int tile);
+
+template <typename T>
+SmemPlan make_plan(int na, bool adjoint, bool with_J = true, int tile = 0) {
+  if (tile <= 0) return make_plan_tile<T>(na, adjoint, with_J, adjoint ? AdjTile<T>::ST : FwdTile<T>::ST);
+  SmemPlan S = make_plan_tile<T>(na, adjoint, with_J, tile);
+  while (S.total > kMaxDynamicSmem && S.st > 4) S = make_plan_tile<T>(na, adjoint, with_J, S.st / 2);
+  return S;
+}
+
+template <typename T>
+SmemPlan make_plan_tile(int na, bool adjoint, bool with_J, int tile) {
   SmemPlan S;
   S.nap = (na + 3) / 4 * 4;
-  S.st = adjoint ? AdjTile<T>::ST : FwdTile<T>::ST;
+  S.st = tile;
+  S.jrow = (S.nap / 4) * (4 * int(sizeof(Jones<T>)) + 16);
   S.npairs = na * (na + 1) / 2;
   S.nitems = count_pair_tiles(na, FwdTile<T>::RP, FwdTile<T>::RQ);
   if (adjoint) {
@@ -93,8 +109,8 @@ SmemPlan make_plan(int na, bool adjoint, bool with_J = true) {
   S.off_ant = take(sizeof(AntInfo<T>) * na);
   S.off_antd = take(0);
   S.off_src = take(sizeof(SrcInfo<T>) * S.st);
-  S.off_J = take(with_J ? sizeof(Jones<T>) * S.st * S.nap : 0);
-  S.off_gJ = take(adjoint ? sizeof(Jones<T>) * S.st * S.nap : 0);
+  S.off_J = take(with_J ? size_t(S.jrow) * S.st : 0);
+  S.off_gJ = take(adjoint ? size_t(S.jrow) * S.st : 0);
   S.off_V = take(adjoint && AdjTile<T>::FULL_Y ? sizeof(T) * size_t(na) * y_row_vals<T>(na)
                                                 : sizeof(Jones<T>) * size_t(S.npairs));
   // FP32 forward: low parts of float-float pair accumulators
@@ -104,6 +120,21 @@ SmemPlan make_plan(int na, bool adjoint, bool with_J = true) {
   S.off_red = take(sizeof(double) * 32);
   S.total = o;
   return S;
+}
+
+// Jones tiles (J and dchi^2/dJ of a source tile) in shared memory: source si,
+// antenna a at byte si * S.jrow + (a / 4) (4 Jones + 16) + (a % 4) Jones.
+// The 16 bytes after every 4 antennas put the 4-antenna blocks that
+// neighbouring lanes read at an odd number of 16-byte bank groups apart, so
+// a quarter warp's 16-byte loads from 8 blocks meet no bank twice.
+template <typename T>
+__device__ __forceinline__ Jones<T>* jtile(Jones<T>* base, const SmemPlan& S, int si, int a) {
+  return reinterpret_cast<Jones<T>*>(reinterpret_cast<unsigned char*>(base) + size_t(si) * S.jrow +
+                                     (a >> 2) * (4 * sizeof(Jones<T>) + 16) + (a & 3) * sizeof(Jones<T>));
+}
+template <typename T>
+__device__ __forceinline__ const Jones<T>* jtile(const Jones<T>* base, const SmemPlan& S, int si, int a) {
+  return jtile(const_cast<Jones<T>*>(base), S, si, a);
 }
 
 // ---------------------------------------------------------------------------
@@ -199,7 +230,7 @@ __device__ __forceinline__ Jones<T> compute_jones(const FusedArgs<T>& A, int t, 
   return jmul(E, KB);
 }
 
-// J(s, a) for the tile into sJ[si * nap + a]; padded antennas get zeros.
+// J(s, a) for the tile into the Jones tile sJ; padded antennas get zeros.
 template <typename T>
 __device__ void produce_jones(const FusedArgs<T>& A, const SmemPlan& S, int t, int ch, int s0, int ns,
                               const SrcInfo<T>* ss, const AntInfo<T>* sa, Jones<T>* sJ, const ChanPos<T>& cp) {
@@ -207,7 +238,8 @@ __device__ void produce_jones(const FusedArgs<T>& A, const SmemPlan& S, int t, i
   const double nu_over_c = double(f) / kLightSpeed;
   for (int i = threadIdx.x; i < ns * S.nap; i += blockDim.x) {
     int si = i / S.nap, a = i - si * S.nap;
-    sJ[i] = a < A.na ? compute_jones(A, t, s0 + si, a, ss[si], sa[a], f, nu_over_c, cp, ch) : jzero<T>();
+    *jtile(sJ, S, si, a) = a < A.na ? compute_jones(A, t, s0 + si, a, ss[si], sa[a], f, nu_over_c, cp, ch)
+                                    : jzero<T>();
   }
 }
 
@@ -372,9 +404,9 @@ __device__ void consume_pairs(const FusedArgs<T>& A, const SmemPlan& S, int ns, 
       for (int si = g; si < ns; si += S.groups) {
         Jones<T> Ja[RP], Jb[RQ];
 #pragma unroll
-        for (int r = 0; r < RP; ++r) Ja[r] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + p0 + r));
+        for (int r = 0; r < RP; ++r) Ja[r] = jload<T>(reinterpret_cast<const T*>(jtile(sJ, S, si, p0 + r)));
 #pragma unroll
-        for (int c = 0; c < RQ; ++c) Jb[c] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + q0 + c));
+        for (int c = 0; c < RQ; ++c) Jb[c] = jload<T>(reinterpret_cast<const T*>(jtile(sJ, S, si, q0 + c)));
         if (!extended) {
 #pragma unroll
           for (int r = 0; r < RP; ++r)
@@ -907,7 +939,7 @@ __device__ void adj_consume_point_full(const FusedArgs<T>& A, const SmemPlan& S,
 #pragma unroll
         for (int c = 0; c < TS; ++c) {
           const int si = min(sb + c, ns - 1);
-          J[c] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + b));
+          J[c] = jload<T>(reinterpret_cast<const T*>(jtile(sJ, S, si, b)));
         }
 #pragma unroll
         for (int r = 0; r < TA; ++r)
@@ -933,7 +965,7 @@ __device__ void adj_consume_point_full(const FusedArgs<T>& A, const SmemPlan& S,
       for (int r = 0; r < TA; ++r)
 #pragma unroll
         for (int c = 0; c < TS; ++c)
-          if (((r * TS + c) & (NB - 1)) == bq && sb + c < ns) sgJ[(sb + c) * S.nap + a0 + r] = acc[r][c];
+          if (((r * TS + c) & (NB - 1)) == bq && sb + c < ns) *jtile(sgJ, S, sb + c, a0 + r) = acc[r][c];
     }
   }
 }
@@ -1121,7 +1153,7 @@ __device__ void adj_consume_point(const FusedArgs<T>& A, const SmemPlan& S, int 
 #pragma unroll
       for (int c = 0; c < RS; ++c) {
         int si = min(sbase + c, ns - 1);
-        Jb[c] = jload<T>(reinterpret_cast<const T*>(sJ + si * S.nap + b));
+        Jb[c] = jload<T>(reinterpret_cast<const T*>(jtile(sJ, S, si, b)));
       }
 #pragma unroll
       for (int r = 0; r < RA; ++r)
@@ -1132,7 +1164,7 @@ __device__ void adj_consume_point(const FusedArgs<T>& A, const SmemPlan& S, int 
     for (int r = 0; r < RA; ++r)
 #pragma unroll
       for (int c = 0; c < RS; ++c)
-        if (sbase + c < ns) sgJ[(sbase + c) * S.nap + a0 + r] = acc[r][c];
+        if (sbase + c < ns) *jtile(sgJ, S, sbase + c, a0 + r) = acc[r][c];
   }
 }
 
@@ -1175,12 +1207,11 @@ __device__ void adj_consume_ext(const FusedArgs<T>& A, const SmemPlan& S, int ns
     T g[3] = {T(0), T(0), T(0)};
     if (active) {
       const SrcInfo<T>& src = ss[si];
-      const Jones<T>* Js = sJ + si * S.nap;
-      const Jones<T> Ja = Js[a];
+      const Jones<T> Ja = *jtile(sJ, S, si, a);
       const T ua = sa[a].u, va = sa[a].v;
       Jones<T> acc = jzero<T>();
       for (int b = 0; b < A.na; ++b) {
-        const Jones<T> P = jmul(y_at(sX, a, b, A.na), Js[b]);
+        const Jones<T> P = jmul(y_at(sX, a, b, A.na), *jtile(sJ, S, si, b));
         T d[3];
         const T c = shape_and_grad<T>(src.type, sa[b].u - ua, sa[b].v - va, src.s0, src.s1, src.s2, kg, ks, d);
         acc = jadd(acc, jscale(P, c));
@@ -1189,7 +1220,7 @@ __device__ void adj_consume_ext(const FusedArgs<T>& A, const SmemPlan& S, int ns
           g[0] += gc * d[0]; g[1] += gc * d[1]; g[2] += gc * d[2];
         }
       }
-      sgJ[si * S.nap + a] = acc;
+      *jtile(sgJ, S, si, a) = acc;
     }
     warp_keyed_add<T, 3>(sacc, 7, active ? si : -1, g);
   }
@@ -1286,7 +1317,7 @@ __device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int c
     const int si = active ? i / A.na : 0, a = active ? i - si * A.na : 0;
     T g[7] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
     if (active)
-      chain_item(A, t, ch, s0 + si, a, ss[si], sa[a], sgJ[si * S.nap + a], f, nu_over_c, half_log_ratio, cp, g);
+      chain_item(A, t, ch, s0 + si, a, ss[si], sa[a], *jtile(sgJ, S, si, a), f, nu_over_c, half_log_ratio, cp, g);
     warp_keyed_add<T, 7>(sacc, 0, active ? si : -1, g);
   }
 }
@@ -1939,6 +1970,8 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.partial_out = d->nsrc.upper_extent < d->nsrc.global_size;
   A.weights = options & MB_APPLY_WEIGHTS;
   A.residuals = options & MB_RESIDUALS;
+  A.src_tile = 4 << ((options & MB_SOURCE_TILE_MASK) >> MB_SOURCE_TILE_SHIFT);  // 8, 16, 32
+  if (!(options & MB_SOURCE_TILE_MASK)) A.src_tile = 0;
   A.want_grad = want_grad;
   A.ll = T(P->beam_ll); A.lmm = T(P->beam_lm); A.ul = T(P->beam_ul); A.um = T(P->beam_um);
   A.lfreq = T(P->beam_lfreq); A.ufreq = T(P->beam_ufreq);
@@ -1992,7 +2025,8 @@ mb_status check_inputs(const mb_dims* d, const mb_props* P, uint32_t options, co
     MB_REQUIRE(in->G_term, "G_term"); MB_REQUIRE(in->flag, "flag"); MB_REQUIRE(in->observed_vis, "observed_vis");
     if (options & MB_APPLY_WEIGHTS) MB_REQUIRE(in->weight_vector, "weight_vector");
   }
-  if (options & ~(MB_APPLY_WEIGHTS | MB_RESIDUALS)) return fail(MB_ERR_INVALID_ARG, "unknown option bits 0x%x", options);
+  if (options & ~(MB_APPLY_WEIGHTS | MB_RESIDUALS | MB_SOURCE_TILE_MASK))
+    return fail(MB_ERR_INVALID_ARG, "unknown option bits 0x%x", options);
   if (!(P->sigma_sqrd > 0.0) && !(options & MB_APPLY_WEIGHTS))
     return fail(MB_ERR_INVALID_ARG, "sigma_sqrd must be > 0 (got %g)", P->sigma_sqrd);
   if (ext(d->na) > 0xffff) return fail(MB_ERR_UNSUPPORTED, "na > 65535");
@@ -2054,7 +2088,7 @@ mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2,
   const size_t row_bytes = mode == MB_MODE_SPLIT_TF32 ? TcGeom<MB_MODE_SPLIT_TF32>::kRowBytes
                                                       : TcGeom<MB_MODE_SPLIT_BF16>::kRowBytes;
   const size_t stage_bytes = size_t(kTcStages) * 2 * 128 * row_bytes;
-  const size_t jbytes = align_up(sizeof(Jones<float>) * S.st * S.nap, 128);
+  const size_t jbytes = align_up(size_t(S.jrow) * S.st, 128);
   const size_t vbytes = sizeof(Jones<float>) * S.npairs;
   size_t o = 0;
   auto take = [&o](size_t b) { size_t r = o; o = align_up(o + b, 128); return r; };
@@ -2105,8 +2139,8 @@ mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* 
   }
   const FusedArgs<T>& B = A;
   constexpr int RP = FwdTile<T>::RP, RQ = FwdTile<T>::RQ;
-  SmemPlan S = make_plan<T>(A.na, false);
-  if (S.total > 227 * 1024)
+  SmemPlan S = make_plan<T>(A.na, false, true, A.src_tile);
+  if (S.total > kMaxDynamicSmem)
     return fail(MB_ERR_UNSUPPORTED, "fused forward needs %zu bytes of shared memory for na=%d (max 232448)",
                 S.total, A.na);
   auto kern = coh_fwd_kernel<T, RP, RQ>;
@@ -2152,7 +2186,7 @@ mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
   }
   if (A.nsrc > A.npsrc) {
     A.sbeg = A.npsrc;
-    SmemPlan S = make_plan<float>(A.na, true);
+    SmemPlan S = make_plan<float>(A.na, true, true, A.src_tile);
     auto kern = coh_adj_kernel<float, AdjTile<float>::RA, AdjTile<float>::RS>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
     { KernelScope ks_("coh_adj_kernel", stream); kern<<<units, S.nthreads, S.total, stream>>>(A, S); }
@@ -2176,8 +2210,8 @@ mb_status launch_adjoint(const FusedArgs<T>& A, mb_mode mode, double grad_scale,
   }
   if (units > 0 && A.nsrc > 0 && !done_sources) {
     constexpr int RA = AdjTile<T>::RA, RS = AdjTile<T>::RS;
-    SmemPlan S = make_plan<T>(A.na, true);
-    if (S.total > 227 * 1024)
+    SmemPlan S = make_plan<T>(A.na, true, true, A.src_tile);
+    if (S.total > kMaxDynamicSmem)
       return fail(MB_ERR_UNSUPPORTED, "fused adjoint needs %zu bytes of shared memory for na=%d", S.total, A.na);
     auto kern = coh_adj_kernel<T, RA, RS>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
@@ -2254,8 +2288,8 @@ mb_status launch_forward_noalloc(FusedArgs<T> A, double* partials, double* X2, c
     return check_launch("sum_partials_kernel");
   }
   constexpr int RP = FwdTile<T>::RP, RQ = FwdTile<T>::RQ;
-  SmemPlan S = make_plan<T>(A.na, false);
-  if (S.total > 227 * 1024)
+  SmemPlan S = make_plan<T>(A.na, false, true, A.src_tile);
+  if (S.total > kMaxDynamicSmem)
     return fail(MB_ERR_UNSUPPORTED, "fused forward needs %zu bytes of shared memory for na=%d (max 232448)",
                 S.total, A.na);
   auto kern = coh_fwd_kernel<T, RP, RQ>;

@@ -16,6 +16,7 @@ struct FusedArgs {
   int lw, mh, nud;
   int t0, ch0;  // first (time, channel) unit handled by this launch
   int sbeg;     // first source handled by the CUDA-core adjoint
+  int src_tile; // requested sources per tile of the CUDA-core kernels (0: default)
   bool accumulate_in, partial_out, weights, residuals, want_grad;
   T ll, lmm, ul, um, lfreq, ufreq, lscale, mscale, gauss_scale, two_pi_over_c;
   double inv_sigma2;
@@ -66,6 +67,7 @@ struct SmemPlan {
   int nitems;       // pair tiles
   int nthreads;     // threads per CTA
   int groups;       // source groups sharing each pair tile (forward)
+  int jrow;         // bytes per source row of the Jones tiles (see jtile)
   size_t off_ant, off_antd, off_src, off_J, off_gJ, off_V, off_Vlo, off_items, off_acc, off_red, total;
 };
 

@@ -41,6 +41,8 @@ class RimeProblem(object):
         self.beam = tuple(int(x) for x in arrays['E_beam'].shape[:3])
         self._ws = {}
         self._x2 = torch.zeros(1, dtype=torch.float64, device=self.device)
+        # sources per shared-memory tile of the CUDA-core kernels (0: default)
+        self.source_tile = 0
 
     # ---- construction -----------------------------------------------------
     @classmethod
@@ -87,7 +89,7 @@ class RimeProblem(object):
         return _cabi.make_props(**self.props)
 
     def options(self):
-        o = 0
+        o = _cabi.source_tile_bits(self.source_tile)
         if self.use_weight_vector:
             o |= _cabi.MB_APPLY_WEIGHTS
         if self.residuals:

@@ -50,12 +50,14 @@ def test_batch_matches_single_problems(dtype, form):
 
 def test_graph_replay_and_autotune():
     import torch
-    from montblanc_gb300.batch import FORMS, RimeBatch, make_sets
+    from montblanc_gb300.batch import CANDIDATES, FORMS, RimeBatch, make_sets
     P = _observation()
     sets = make_sets(P, 6, seed=2, lo=3, hi=60)
     b = RimeBatch(P, sets, dtype='float')
     forms = b.autotune()
     assert len(forms) == 6 and all(f in FORMS for f in forms)
+    assert all(c in CANDIDATES for c in zip(b.forms, b.tiles))
+    assert all(len(v) == len(CANDIDATES) for v in b.tune_times.values())
     eager = b.run().clone()
     g_eager = {k: v.clone() for k, v in b.grads.items()}
     b.capture()
@@ -68,3 +70,25 @@ def test_graph_replay_and_autotune():
     assert torch.equal(replay, eager)
     for k in g_eager:
         assert torch.allclose(b.grads[k], g_eager[k], rtol=1e-5, atol=1e-6 * float(g_eager[k].abs().max() + 1e-30))
+
+
+@pytest.mark.parametrize('dtype,form,tile', [('float', 'native', 8), ('float', 'native', 32),
+                                             ('double', 'native', 32), ('float', 'split_tf32', 8)])
+def test_source_tiles_leave_results_unchanged(dtype, form, tile):
+    """The source tile of the CUDA-core kernels only changes the order of
+    summation."""
+    from montblanc_gb300.batch import RimeBatch, make_sets
+    P = _observation()
+    sets = make_sets(P, 3, seed=5, lo=20, hi=70)
+    a = RimeBatch(P, sets, dtype=dtype)
+    b = RimeBatch(P, sets, dtype=dtype)
+    a.forms = b.forms = [form] * 3
+    b.tiles = [tile] * 3
+    xa, xb = a.run().cpu().numpy(), b.run().cpu().numpy()
+    tol = 1e-12 if dtype == 'double' else 2e-6
+    assert np.all(np.abs(xa - xb) <= tol * np.abs(xa))
+    for i in range(3):
+        ga, gb = a.set_grads(i), b.set_grads(i)
+        for k in ('lm', 'stokes', 'gauss_shape', 'sersic_shape'):
+            if ga[k].size:
+                assert np.abs(ga[k] - gb[k]).max() <= 10 * tol * max(np.abs(ga[k]).max(), 1e-30), (i, k)
