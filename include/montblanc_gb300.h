@@ -59,8 +59,9 @@ typedef enum mb_mode {
 /* Source tile of the CUDA-core coherency kernels (the native forms and the
  * extended sources' adjoint of the split forms): sources per shared-memory
  * tile, a tuning hint that does not change results beyond rounding order.
- * 0 keeps the default (16 in FP32, 8 in FP64); a tile whose shared memory
- * does not fit is halved until it does. */
+ * 0 keeps the default (16 in FP32, 8 in FP64; 32 for the split forms'
+ * extended-source adjoint); a tile whose shared memory does not fit is
+ * halved until it does. */
 #define MB_SOURCE_TILE_SHIFT 8
 #define MB_SOURCE_TILE_MASK (0x3u << MB_SOURCE_TILE_SHIFT)
 #define MB_SOURCE_TILE_8 (0x1u << MB_SOURCE_TILE_SHIFT)

@@ -33,7 +33,7 @@ FORMS = ('native', 'split_tf32')
 #: (form, source tile) pairs the autotuner times by default; tile 0 is the
 #: library default.  The tile only concerns the CUDA-core kernels: all of a
 #: native set, the extended sources' adjoint of a split set.
-CANDIDATES = (('native', 8), ('native', 16), ('native', 32), ('split_tf32', 0), ('split_tf32', 32))
+CANDIDATES = (('native', 8), ('native', 16), ('native', 32), ('split_tf32', 0), ('split_tf32', 16))
 
 
 def make_sets(P, nsets, seed=0, lo=10, hi=5000, gauss_fraction=0.16, sersic_fraction=0.04):

@@ -71,22 +71,25 @@ int count_pair_tiles(int na, int RP, int RQ) {
   return n;
 }
 
-// with_J = false leaves out the Jones tile (a caller that places it itself).
-// tile > 0 asks for that many sources per tile; the tile is halved (down to
-// 4) while the plan does not fit the shared memory of one CTA.
+// with_J = false leaves out the Jones tile (a caller that places it itself),
+// with_gJ = false the adjoint's dchi^2/dJ tile (launches of extended sources
+// only, which chain each item where it is formed).  tile > 0 asks for that
+// many sources per tile; the tile is halved (down to 4) while the plan does
+// not fit the shared memory of one CTA.
 template <typename T>
-SmemPlan make_plan_tile(int na, bool adjoint, bool with_J, int tile);
+SmemPlan make_plan_tile(int na, bool adjoint, bool with_J, int tile, bool with_gJ);
 
 template <typename T>
-SmemPlan make_plan(int na, bool adjoint, bool with_J = true, int tile = 0) {
-  if (tile <= 0) return make_plan_tile<T>(na, adjoint, with_J, adjoint ? AdjTile<T>::ST : FwdTile<T>::ST);
-  SmemPlan S = make_plan_tile<T>(na, adjoint, with_J, tile);
-  while (S.total > kMaxDynamicSmem && S.st > 4) S = make_plan_tile<T>(na, adjoint, with_J, S.st / 2);
+SmemPlan make_plan(int na, bool adjoint, bool with_J = true, int tile = 0, bool with_gJ = true) {
+  if (tile <= 0)
+    return make_plan_tile<T>(na, adjoint, with_J, adjoint ? AdjTile<T>::ST : FwdTile<T>::ST, with_gJ);
+  SmemPlan S = make_plan_tile<T>(na, adjoint, with_J, tile, with_gJ);
+  while (S.total > kMaxDynamicSmem && S.st > 4) S = make_plan_tile<T>(na, adjoint, with_J, S.st / 2, with_gJ);
   return S;
 }
 
 template <typename T>
-SmemPlan make_plan_tile(int na, bool adjoint, bool with_J, int tile) {
+SmemPlan make_plan_tile(int na, bool adjoint, bool with_J, int tile, bool with_gJ) {
   SmemPlan S;
   S.nap = (na + 3) / 4 * 4;
   S.st = tile;
@@ -110,7 +113,7 @@ SmemPlan make_plan_tile(int na, bool adjoint, bool with_J, int tile) {
   S.off_antd = take(0);
   S.off_src = take(sizeof(SrcInfo<T>) * S.st);
   S.off_J = take(with_J ? size_t(S.jrow) * S.st : 0);
-  S.off_gJ = take(adjoint ? size_t(S.jrow) * S.st : 0);
+  S.off_gJ = take(adjoint && with_gJ ? size_t(S.jrow) * S.st : 0);
   S.off_V = take(adjoint && AdjTile<T>::FULL_Y ? sizeof(T) * size_t(na) * y_row_vals<T>(na)
                                                 : sizeof(Jones<T>) * size_t(S.npairs));
   // FP32 forward: low parts of float-float pair accumulators
@@ -1191,41 +1194,6 @@ __device__ __forceinline__ void warp_keyed_add(T* acc, int first, int key, T (&v
   }
 }
 
-// dJ_a(s) = sum_b shape_s(a, b) Y_ab J_b(s) for the extended sources of a
-// tile, with d chi^2 / d(shape parameters) from the pairs a < b.  Work item
-// (source, antenna a); the lanes of a warp take consecutive antennas.
-template <typename T>
-__device__ void adj_consume_ext(const FusedArgs<T>& A, const SmemPlan& S, int ns, const SrcInfo<T>* ss,
-                                const AntInfo<T>* sa, const Jones<T>* sJ, const Jones<T>* sX, Jones<T>* sgJ,
-                                T* sacc, T kg, T ks) {
-  const int n = ns * A.na;
-  const int rounds = (n + blockDim.x - 1) / blockDim.x;
-  for (int round = 0; round < rounds; ++round) {
-    const int k = round * blockDim.x + threadIdx.x;
-    const bool active = k < n;
-    const int si = active ? k / A.na : 0, a = active ? k - si * A.na : 0;
-    T g[3] = {T(0), T(0), T(0)};
-    if (active) {
-      const SrcInfo<T>& src = ss[si];
-      const Jones<T> Ja = *jtile(sJ, S, si, a);
-      const T ua = sa[a].u, va = sa[a].v;
-      Jones<T> acc = jzero<T>();
-      for (int b = 0; b < A.na; ++b) {
-        const Jones<T> P = jmul(y_at(sX, a, b, A.na), *jtile(sJ, S, si, b));
-        T d[3];
-        const T c = shape_and_grad<T>(src.type, sa[b].u - ua, sa[b].v - va, src.s0, src.s1, src.s2, kg, ks, d);
-        acc = jadd(acc, jscale(P, c));
-        if (a < b) {
-          const T gc = jdot_re(Ja, P);
-          g[0] += gc * d[0]; g[1] += gc * d[1]; g[2] += gc * d[2];
-        }
-      }
-      *jtile(sgJ, S, si, a) = acc;
-    }
-    warp_keyed_add<T, 3>(sacc, 7, active ? si : -1, g);
-  }
-}
-
 // Chain d chi^2 / dJ(s, a) through E and K: d chi^2 / d(l, m) of the item
 // and gB = d chi^2 / d sqrt(B) (complex, per Jones entry).  Uses src.l, m,
 // l_over_n, m_over_n and B.
@@ -1322,6 +1290,53 @@ __device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int c
   }
 }
 
+// Extended sources of a tile, consumed and chained in one pass: work item
+// (source, antenna a), the lanes of a warp taking consecutive antennas,
+// forms dJ_a(s) = sum_b shape_s(a, b) Y_ab J_b(s) with d chi^2 / d(shape
+// parameters) from the pairs a < b, and chains dJ_a(s) through E, K and
+// sqrt(B) to the source's l, m, I, Q, U, V, alpha at once (chain_item), so
+// dJ never goes through shared memory.  All 10 per-source sums of an item
+// are added with one keyed warp sum.
+template <typename T>
+__device__ void adj_ext_tile(const FusedArgs<T>& A, const SmemPlan& S, int t, int ch, int s0, int ns,
+                             const SrcInfo<T>* ss, const AntInfo<T>* sa, const Jones<T>* sJ, const Jones<T>* sX,
+                             T* sacc, T kg, T ks, const ChanPos<T>& cp) {
+  const T f = A.freq[ch];
+  const double nu_over_c = double(f) / kLightSpeed;
+  const T half_log_ratio = T(0.5) * mb_log(f / A.ref_freq[ch]);
+  const int n = ns * A.na;
+  const int rounds = (n + blockDim.x - 1) / blockDim.x;
+  for (int round = 0; round < rounds; ++round) {
+    const int k = round * blockDim.x + threadIdx.x;
+    const bool active = k < n;
+    const int si = active ? k / A.na : 0, a = active ? k - si * A.na : 0;
+    T g[kNAcc];
+#pragma unroll
+    for (int e = 0; e < kNAcc; ++e) g[e] = T(0);
+    if (active) {
+      const SrcInfo<T>& src = ss[si];
+      const Jones<T> Ja = *jtile(sJ, S, si, a);
+      const T ua = sa[a].u, va = sa[a].v;
+      Jones<T> acc = jzero<T>();
+      for (int b = 0; b < A.na; ++b) {
+        const Jones<T> P = jmul(y_at(sX, a, b, A.na), *jtile(sJ, S, si, b));
+        T d[3];
+        const T c = shape_and_grad<T>(src.type, sa[b].u - ua, sa[b].v - va, src.s0, src.s1, src.s2, kg, ks, d);
+        acc = jadd(acc, jscale(P, c));
+        if (a < b) {
+          const T gc = jdot_re(Ja, P);
+          g[7] += gc * d[0]; g[8] += gc * d[1]; g[9] += gc * d[2];
+        }
+      }
+      T gc7[7];
+      chain_item(A, t, ch, s0 + si, a, src, sa[a], acc, f, nu_over_c, half_log_ratio, cp, gc7);
+#pragma unroll
+      for (int e = 0; e < 7; ++e) g[e] = gc7[e];
+    }
+    warp_keyed_add<T, kNAcc>(sacc, 0, active ? si : -1, g);
+  }
+}
+
 template <typename T>
 __device__ void adj_flush(const FusedArgs<T>& A, int t, int s0, int ns, T* sacc) {
   for (int i = threadIdx.x; i < ns * kNAcc; i += blockDim.x) {
@@ -1387,10 +1402,11 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
     if (s0 < A.npsrc) {
       if (AdjTile<T>::FULL_Y) adj_consume_point_full<T>(A, S, ns, sJ, sX, sgJ);
       else adj_consume_point<T, RA, RS>(A, S, ns, sJ, sX, sgJ);
+      __syncthreads();
+      adj_chain<T>(A, S, t, ch, s0, ns, ss, sa, sgJ, sacc, cp);
+    } else {
+      adj_ext_tile<T>(A, S, t, ch, s0, ns, ss, sa, sJ, sX, sacc, kg, ks, cp);
     }
-    else adj_consume_ext<T>(A, S, ns, ss, sa, sJ, sX, sgJ, sacc, kg, ks);
-    __syncthreads();
-    adj_chain<T>(A, S, t, ch, s0, ns, ss, sa, sgJ, sacc, cp);
     __syncthreads();
     adj_flush<T>(A, t, s0, ns, sacc);
     __syncthreads();
@@ -2186,7 +2202,8 @@ mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
   }
   if (A.nsrc > A.npsrc) {
     A.sbeg = A.npsrc;
-    SmemPlan S = make_plan<float>(A.na, true, true, A.src_tile);
+    // extended sources only: no dchi^2/dJ tile, 32-source tiles by default
+    SmemPlan S = make_plan<float>(A.na, true, true, A.src_tile ? A.src_tile : 32, false);
     auto kern = coh_adj_kernel<float, AdjTile<float>::RA, AdjTile<float>::RS>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
     { KernelScope ks_("coh_adj_kernel", stream); kern<<<units, S.nthreads, S.total, stream>>>(A, S); }
