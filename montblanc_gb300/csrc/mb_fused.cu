@@ -537,23 +537,17 @@ struct TcPlan {
   int group;
 };
 
-__device__ __forceinline__ void fold_scalar(float* hi, float* lo, float x) {
-  float a = *hi;
-  float sum = a + x;
-  float bp = sum - a;
-  float err = (a - (sum - bp)) + (x - bp);
-  *hi = sum;
-  *lo += err;
-}
-
-// The same with the low part kept in BF16: it only carries the rounding
-// errors of the high part (a few ulp of it), which 8 significant bits hold
-// to far below an ulp of the sum.
+// Float-float accumulation of a drained group sum x into (hi, lo), the low
+// part in BF16: it only carries the rounding errors of the high part (a few
+// ulp of it), which 8 significant bits hold to far below an ulp of the sum.
+// Fast2Sum: the error term x - ((hi + x) - hi) is exact when |hi| >= |x|,
+// the usual case (hi is the sum over all earlier groups; also exact while hi
+// is 0); otherwise it is off by at most an ulp of the sum, the error of one
+// plain FP32 addition.
 __device__ __forceinline__ void fold_scalar(float* hi, __nv_bfloat16* lo, float x) {
-  float a = *hi;
-  float sum = a + x;
-  float bp = sum - a;
-  float err = (a - (sum - bp)) + (x - bp);
+  const float a = *hi;
+  const float sum = a + x;
+  const float err = x - (sum - a);
   *hi = sum;
   *lo = __float2bfloat16_rn(__bfloat162float(*lo) + err);
 }
@@ -1456,8 +1450,12 @@ constexpr uint32_t kTaGroupCols = 64;
 constexpr uint32_t kTaCols = 512;
 static_assert(kTaYCols + kTaGroups * kTaGroupCols <= kTaCols, "TMEM columns of Y and the worker groups");
 constexpr int kTaPark = 6;            // float4 of parked state per item
-constexpr int kTaAcc = 10;            // per-source sums: d/dl, d/dm, gB (8)
-static_assert(kTaAcc <= 16, "per-source sums fit the 16-lane reduce-scatter");
+// Per-source sums: d/dl, d/dm and the Hermitian part of gB = d chi^2 /
+// d sqrt(B) that the Stokes and alpha gradients depend on (sqrt(B) is
+// Hermitian with real diagonal): Re gB00, Re gB11, Re (gB01 + gB10),
+// Im (gB01 - gB10).
+constexpr int kTaAcc = 6;
+static_assert(kTaAcc <= 8, "per-source sums fit the 8-value reduce-scatter");
 using TaGeom = StageGeometry<kTaRowBytes>;
 using TaLayout = StageLayout<MB_MODE_SPLIT_BF16, kTaRowBytes>;
 constexpr size_t kYopBytes = 2 * size_t(TaGeom::kMatBytes);          // hi + lo: 128 KB
@@ -1506,29 +1504,27 @@ __global__ void yop_build_kernel(FusedArgs<float> A) {
 }
 
 // Sum of v[k] over the 16 lanes that share lane bit 0, by reduce-scatter
-// over lane bits 4, 3, 2, 1 (15 shuffles for 16 values).  Afterwards the
-// lane whose bits 4..1 read k holds the sum of value k; *k is returned.
-__device__ __forceinline__ float reduce_scatter16(const float (&v)[16], int lane, int* k) {
-  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4, b1 = lane & 2;
-  float w8[8], w4[4], w2[2];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const float r = __shfl_xor_sync(0xffffffffu, b4 ? v[j] : v[j + 8], 16);
-    w8[j] = (b4 ? v[j + 8] : v[j]) + r;
-  }
+// over lane bits 4, 3, 2 and a plain sum over bit 1 (8 shuffles for 8
+// values).  Afterwards both lanes whose bits 4..2 read k hold the sum of
+// value k; *k is returned.
+__device__ __forceinline__ float reduce_scatter8(const float (&w8)[8], int lane, int* k) {
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  float w4[4], w2[2];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const float r = __shfl_xor_sync(0xffffffffu, b3 ? w8[j] : w8[j + 4], 8);
-    w4[j] = (b3 ? w8[j + 4] : w8[j]) + r;
+    const float r = __shfl_xor_sync(0xffffffffu, b4 ? w8[j] : w8[j + 4], 16);
+    w4[j] = (b4 ? w8[j + 4] : w8[j]) + r;
   }
 #pragma unroll
   for (int j = 0; j < 2; ++j) {
-    const float r = __shfl_xor_sync(0xffffffffu, b2 ? w4[j] : w4[j + 2], 4);
-    w2[j] = (b2 ? w4[j + 2] : w4[j]) + r;
+    const float r = __shfl_xor_sync(0xffffffffu, b3 ? w4[j] : w4[j + 2], 8);
+    w2[j] = (b3 ? w4[j + 2] : w4[j]) + r;
   }
-  const float r = __shfl_xor_sync(0xffffffffu, b1 ? w2[0] : w2[1], 2);
-  *k = (b4 ? 8 : 0) + (b3 ? 4 : 0) + (b2 ? 2 : 0) + (b1 ? 1 : 0);
-  return (b1 ? w2[1] : w2[0]) + r;
+  const float r = __shfl_xor_sync(0xffffffffu, b2 ? w2[0] : w2[1], 4);
+  float x = (b2 ? w2[1] : w2[0]) + r;
+  x += __shfl_xor_sync(0xffffffffu, x, 2);
+  *k = (b4 ? 4 : 0) + (b3 ? 2 : 0) + (b2 ? 1 : 0);
+  return x;
 }
 
 // Barrier over the 4 warps of worker group `grp` (ids 1, 2) that ORs a
@@ -1763,9 +1759,9 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
         Jones<float> gJ;
         gJ.a = i ? p0 : o0; gJ.b = i ? p1 : o1;
         gJ.c = i ? o0 : p0; gJ.d = i ? o1 : p1;
-        float gsum[16];  // kTaAcc values, zero padded for the reduce-scatter
+        float gsum[8];  // kTaAcc values, zero padded for the reduce-scatter
 #pragma unroll
-        for (int e = 0; e < 16; ++e) gsum[e] = 0.f;
+        for (int e = 0; e < 8; ++e) gsum[e] = 0.f;
         float sv[24];  // parked EK, Pl, Pm of the item
 #pragma unroll
         for (int x = 0; x < kTaPark; ++x) {
@@ -1793,14 +1789,15 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
                     gphi * (ai.u - ai.w * src.l_over_n);
           gsum[1] = -g_ld * ai.sc_l * ai.sin_pa + g_md * ai.sc_m * ai.cos_pa +
                     gphi * (ai.v - ai.w * src.m_over_n);
-          const float* gb = reinterpret_cast<const float*>(&gB);
-#pragma unroll
-          for (int e = 0; e < 8; ++e) gsum[2 + e] = gb[e];
+          gsum[2] = gB.a.r;
+          gsum[3] = gB.d.r;
+          gsum[4] = gB.b.r + gB.c.r;
+          gsum[5] = gB.b.i - gB.c.i;
         }
         // sum over the warp's 16 antennas (lane bits 1-4)
         int e;
-        const float x = reduce_scatter16(gsum, lane, &e);
-        if (e < kTaAcc) atomicAdd(acc + sl * kTaAcc + e, x);
+        const float x = reduce_scatter8(gsum, lane, &e);
+        if (e < kTaAcc && !(lane & 2)) atomicAdd(acc + sl * kTaAcc + e, x);
       }
       if (group_sync_or(grp, bad)) { bad = true; break; }
       // flush the tile's per-source sums to the FP64 accumulators; the
@@ -1813,10 +1810,9 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
           if (rr[0] != 0.f) atomicAdd(&A.acc_lm[2 * sg], double(rr[0]));
           if (rr[1] != 0.f) atomicAdd(&A.acc_lm[2 * sg + 1], double(rr[1]));
           const SrcInfo<float> src = point_source_stokes(A, t, ch, sg, log2_ratio);
-          Jones<float> gB;
-          float* gb = reinterpret_cast<float*>(&gB);
-#pragma unroll
-          for (int e = 0; e < 8; ++e) gb[e] = rr[2 + e];
+          // a Hermitian gB with the summed parts (all the gradients read)
+          const Jones<float> gB = {{rr[2], 0.f}, {0.5f * rr[4], 0.5f * rr[5]}, {0.5f * rr[4], -0.5f * rr[5]},
+                                   {rr[3], 0.f}};
           float gs[5];
           stokes_grads(src, gB, half_log_ratio, gs);
           double* st = &A.acc_stokes[(size_t(sg) * A.ntime + t) * 4];
