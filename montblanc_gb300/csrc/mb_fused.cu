@@ -607,15 +607,6 @@ __device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, _
   }
 }
 
-// Prefetch into L1 the per-item table entries of point source s at time t
-// and antenna a (sqrt(B) table, direction, FP64 path length), a tile before
-// they are read.
-__device__ __forceinline__ void prefetch_point_item(const FusedArgs<float>& A, int t, int s, int a) {
-  if (A.bsq0) tc::prefetch_l1(A.bsq0 + kBsqVals * (size_t(s) * A.ntime + t));
-  tc::prefetch_l1(A.lm + 2 * s);
-  if (A.phi) tc::prefetch_l1(A.phi + (size_t(t) * A.nsrc + s) * A.na + a);
-}
-
 // Source terms needed for a point source's J at (time t, channel ch).
 __device__ __forceinline__ SrcInfo<float> point_source_info(const FusedArgs<float>& A, int t, int ch, int s,
                                                            float log2_ratio) {
@@ -1541,8 +1532,22 @@ __device__ __forceinline__ bool group_sync_or(int grp, bool x) {
 }
 
 struct TaPlan {
-  size_t off_park, off_stage, off_ant, off_acc, off_bar, total;
+  size_t off_park, off_stage, off_ant, off_acc, off_src, off_bar, total;
 };
+
+// Per-source terms of a tile shared by a worker group's items:
+// sqrt(B) (Re B00, Re B11, Re B01, Im B01; B10 = conj B01) and l, m, l / n,
+// m / n.  Eight lanes fill a tile's entries, a tile ahead.
+struct TaSrc {
+  float4 b, lm;
+};
+
+__device__ __forceinline__ void ta_fill_src(const FusedArgs<float>& A, int t, int ch, int s, float log2_ratio,
+                                            TaSrc* dst) {
+  const SrcInfo<float> si = point_source_chain_info(A, t, ch, s, log2_ratio);
+  dst->b = make_float4(si.B.a.r, si.B.d.r, si.B.b.r, si.B.b.i);
+  dst->lm = make_float4(si.l, si.m, si.l_over_n, si.m_over_n);
+}
 
 // The MMAs of one tile for one chain of dJ = Y J, from the Y operand in
 // TMEM (ytm: column 0, lane 0) and the tile's J operand at jsm (shared-memory
@@ -1582,6 +1587,7 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
   unsigned char* stage = smem + P.off_stage;  // [kTaGroups][kJopBytes]
   AntInfo<float>* sa = reinterpret_cast<AntInfo<float>*>(smem + P.off_ant);
   float* sacc = reinterpret_cast<float*>(smem + P.off_acc);  // [kTaGroups][2][kTaKappa][kTaAcc]
+  TaSrc* ssrc = reinterpret_cast<TaSrc*>(smem + P.off_src);   // [kTaGroups][2][kTaKappa]
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + P.off_bar);
   uint64_t* dfull = bars;               // [kTaGroups] MMA commit -> group (dJ in TMEM)
   uint64_t* done = dfull + kTaGroups;   // [kTaGroups] last MMAs of a group
@@ -1657,15 +1663,33 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
     const float* plane = A.plane ? A.plane + size_t(ch) * A.lw * A.mh * kPlaneVals : nullptr;
     const uint32_t tlane = tmem + (uint32_t(32 * q) << 16) + kTaYCols + uint32_t(kTaGroupCols * grp);
     float4* mypark = park + size_t(grp) * kTaItems * kTaPark * 128 + r;
-    bool bad = false;
+    TaSrc* gsrc = ssrc + size_t(grp) * 2 * kTaKappa;  // this group's two tiles of source terms
+    const int ct = tid - grp * kTaGroupThreads;        // thread index within the group
+    if (ct < kTaKappa && grp < ntiles) {
+      const int s = tile_of(grp) * kTaKappa + ct;
+      if (s < A.npsrc) ta_fill_src(A, t, ch, s, log2_ratio, gsrc + ct);
+    }
+    bool bad = group_sync_or(grp, false);
     int k = 0;  // this group's tile count
     for (int g = grp; g < ntiles; g += kTaGroups, ++k) {
       const int s0 = tile_of(g) * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
-      if (ant_ok && g + kTaGroups < ntiles) {  // the group's next tile
+      const TaSrc* tsrc = gsrc + (k & 1) * kTaKappa;  // this tile's source terms
+      if (ct < kTaKappa && g + kTaGroups < ntiles) {   // the next tile's, before the staging barrier
+        const int s = tile_of(g + kTaGroups) * kTaKappa + ct;
+        if (s < A.npsrc) ta_fill_src(A, t, ch, s, log2_ratio, gsrc + ((k + 1) & 1) * kTaKappa + ct);
+      }
+      if (ant_ok && g + kTaGroups < ntiles && A.phi) {  // the items' path lengths, a tile ahead
         const int sn0 = tile_of(g + kTaGroups) * kTaKappa;
 #pragma unroll
         for (int u = 0; u < kTaItems; ++u)
-          if (sn0 + 4 * i + u < A.npsrc) prefetch_point_item(A, t, sn0 + 4 * i + u, a);
+          if (sn0 + 4 * i + u < A.npsrc) tc::prefetch_l1(A.phi + (size_t(t) * A.nsrc + sn0 + 4 * i + u) * A.na + a);
+      }
+      if (ct < kTaKappa && g + 2 * kTaGroups < ntiles) {  // the source terms' table entries, two tiles ahead
+        const int s = tile_of(g + 2 * kTaGroups) * kTaKappa + ct;
+        if (s < A.npsrc) {
+          if (A.bsq0) tc::prefetch_l1(A.bsq0 + kBsqVals * (size_t(s) * A.ntime + t));
+          tc::prefetch_l1(A.lm + 2 * s);
+        }
       }
       // ---- forward step: J of the items, staged for the MMA -------------
 #pragma unroll
@@ -1677,16 +1701,16 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
         for (int e = 0; e < 8; ++e) st[0][e] = st[1][e] = st[2][e] = 0.f;
         if (!bad && ant_ok && sl < ns) {
           const int sg = s0 + sl;
-          const SrcInfo<float> src = point_source_info(A, t, ch, sg, log2_ratio);
+          const float4 tb = tsrc[sl].b, tlm = tsrc[sl].lm;
           const Cx<float> K = phase_term(A, t, sg, a, f, nu_over_c);
           float l, m;
-          beam_lm<float>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
+          beam_lm<float>(tlm.x, tlm.y, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
           const GridPos<float> gl = grid_pos<float>(l, A.ll, A.ul, A.lscale, A.lw);
           const GridPos<float> gm = grid_pos<float>(m, A.lmm, A.um, A.mscale, A.mh);
           Jones<float> E, dEl, dEm;
           if (plane) beam_interp_plane_d<float>(plane, A.mh, gl, gm, E, dEl, dEm);
           else beam_interp_d<float>(A.E_beam, G, gl, gm, cp, E, dEl, dEm);
-          const Jones<float>& B = src.B;
+          const Jones<float> B = {{tb.x, 0.f}, {tb.z, tb.w}, {tb.z, -tb.w}, {tb.y, 0.f}};
           const Jones<float> KB = {cmul(K, B.a), cmul(K, B.b), cmul(K, B.c), cmul(K, B.d)};
           J = jmul(E, KB);
           const Jones<float> EK = {cmul(E.a, K), cmul(E.b, K), cmul(E.c, K), cmul(E.d, K)};
@@ -1769,8 +1793,7 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
           sv[4 * x] = p4.x; sv[4 * x + 1] = p4.y; sv[4 * x + 2] = p4.z; sv[4 * x + 3] = p4.w;
         }
         if (!bad && ant_ok && sl < ns) {
-          const int sg = s0 + sl;
-          const SrcInfo<float> src = point_source_chain_info(A, t, ch, sg, log2_ratio);
+          const float4 tb = tsrc[sl].b, tlm = tsrc[sl].lm;
           Jones<float> EK, Pl, Pm;
 #pragma unroll
           for (int e = 0; e < 8; ++e) {
@@ -1781,14 +1804,13 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
           const Jones<float> gB = jhmul(EK, gJ);
           const float g_ld = jdot_re(gJ, Pl), g_md = jdot_re(gJ, Pm);
           // Im tr(gB^H B), B = [[a, b], [conj(b), d]] with a, d real
-          const Jones<float>& B = src.B;
-          const float imt = -gB.a.i * B.a.r - gB.d.i * B.d.r + (gB.b.r * B.b.i - gB.b.i * B.b.r) +
-                            (gB.c.r * B.c.i - gB.c.i * B.c.r);
+          const float imt = -gB.a.i * tb.x - gB.d.i * tb.y + (gB.b.r * tb.w - gB.b.i * tb.z) -
+                            (gB.c.r * tb.w + gB.c.i * tb.z);
           const float gphi = dphase * imt;
           gsum[0] = g_ld * ai.sc_l * ai.cos_pa + g_md * ai.sc_m * ai.sin_pa +
-                    gphi * (ai.u - ai.w * src.l_over_n);
+                    gphi * (ai.u - ai.w * tlm.z);
           gsum[1] = -g_ld * ai.sc_l * ai.sin_pa + g_md * ai.sc_m * ai.cos_pa +
-                    gphi * (ai.v - ai.w * src.m_over_n);
+                    gphi * (ai.v - ai.w * tlm.w);
           gsum[2] = gB.a.r;
           gsum[3] = gB.d.r;
           gsum[4] = gB.b.r + gB.c.r;
@@ -1802,7 +1824,6 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
       if (group_sync_or(grp, bad)) { bad = true; break; }
       // flush the tile's per-source sums to the FP64 accumulators; the
       // other accumulator buffer takes the group's next tile
-      const int ct = tid - grp * kTaGroupThreads;
       if (ct < kTaKappa) {
         float* rr = acc + ct * kTaAcc;
         if (ct < ns) {
@@ -2187,6 +2208,7 @@ mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
     P.off_stage = take(size_t(kTaGroups) * kJopBytes);
     P.off_ant = take(sizeof(AntInfo<float>) * A.na);
     P.off_acc = take(sizeof(float) * kTaGroups * 2 * kTaKappa * kTaAcc);
+    P.off_src = take(sizeof(TaSrc) * kTaGroups * 2 * kTaKappa);
     P.off_bar = take(2 * kTaGroups * sizeof(uint64_t) + 16);
     P.total = o;
     MB_CUDA(cudaFuncSetAttribute(coh_tc_adj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
