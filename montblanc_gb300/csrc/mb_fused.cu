@@ -514,7 +514,7 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A,
 constexpr int kTcProducerWarps = 11;       // warps 0-10: operands (one source each), drain
 constexpr int kTcProducers = 32 * kTcProducerWarps;
 constexpr int kTcThreads = kTcProducers + 32;  // warp 11: MMA issue, drain
-constexpr int kTcStages = 2;
+constexpr int kTcStages = 3;                // operand stages in flight
 constexpr int kTcGroup = 6;                // stages per TMEM accumulation group (66 sources)
 // TMEM columns: D_re 0-127, D_im 128-255 (hi.hi); their corrections 256-511.
 constexpr uint32_t kTcCols = 512;
@@ -533,39 +533,43 @@ static_assert(TcGeom<MB_MODE_SPLIT_TF32>::kSlots >= kTcProducerWarps, "a slot pe
 static_assert(TcGeom<MB_MODE_SPLIT_BF16>::kSlots >= kTcProducerWarps, "a slot per producer warp");
 
 struct TcPlan {
-  size_t off_stage, off_vlo16, off_vlo32, off_bar, total;
+  size_t off_stage, off_vlo32, off_bar, total;
   int group;
 };
 
-// Float-float accumulation of a drained group sum x into (hi, lo), the low
-// part in BF16: it only carries the rounding errors of the high part (a few
-// ulp of it), which 8 significant bits hold to far below an ulp of the sum.
-// Fast2Sum: the error term x - ((hi + x) - hi) is exact when |hi| >= |x|,
-// the usual case (hi is the sum over all earlier groups; also exact while hi
-// is 0); otherwise it is off by at most an ulp of the sum, the error of one
-// plain FP32 addition.
-__device__ __forceinline__ void fold_scalar(float* hi, __nv_bfloat16* lo, float x) {
+// Adds a drained group sum x to the pair accumulator *hi and returns the
+// rounding error of the addition.  Fast2Sum: x - ((hi + x) - hi) is exact
+// when |hi| >= |x|, the usual case (hi is the sum over all earlier groups;
+// also exact while hi is 0); otherwise it is off by at most an ulp of the
+// sum, the error of one plain FP32 addition.
+__device__ __forceinline__ float fold_carry(float* hi, float x) {
   const float a = *hi;
   const float sum = a + x;
-  const float err = x - (sum - a);
   *hi = sum;
-  *lo = __float2bfloat16_rn(__bfloat162float(*lo) + err);
+  return x - (sum - a);
 }
 
-// Drain TMEM into the float-float pair accumulators (all 12 warps): a warp
-// reads the 32 TMEM lanes of its quarter (rows 2a + i) and takes every third
-// of the quarter's 8 tasks (D_re or D_im, one block of 16 column antennas).
-// Each unordered antenna pair is drained once, by the row whose cyclic
-// distance to the other is below na / 2 (ties: the smaller index), so every
-// row drains about na / 2 columns and the warps share the work evenly: row a
+// Drain TMEM into the FP32 pair accumulators (all 12 warps): a warp reads
+// the 32 TMEM lanes of its quarter (rows 2a + i) and takes every third of the
+// quarter's 8 tasks (D_re or D_im, one block of 16 column antennas).  Each
+// unordered antenna pair is drained once, by the row whose cyclic distance
+// to the other is below na / 2 (ties: the smaller index), so every row
+// drains about na / 2 columns and the warps share the work evenly: row a
 // drains the antennas b of the cyclic interval [a, a + dmax], b in
 // [a, up_hi] from its own block of V_ab and the wrapped b in [0, wrap_end]
 // as V_ba = (sum J_a J_b^H)^H (transposed, conjugated).
+// Each drained value is main + correction accumulator; the rounding error
+// of adding it to the pair accumulator is written back (carry) into the
+// correction accumulator's entry, which the next group's hi.lo + lo.hi MMAs
+// add to and the next drain of the same entry (by the same lane) folds in.
+// So the pair accumulators together with the correction accumulators hold
+// the sum as a float-float value with no low part in shared memory.  Entries
+// a lane does not fold get a zero carry.
 // Element offsets of the pair accumulators (pair_index(p, q) * 8 + (2 row +
 // col) * 2 + re/im) split into a per-lane part and a part in b and j:
 //   b >= a:  ku + 8 b + 2 j,  ku = 8 (a na - a (a - 1) / 2 - a) + 4 i + h
 //   b <  a:  8 R_b + kl + 4 j,  kl = 8 a + 2 i + h,  R_b = b na - b (b - 1) / 2 - b
-__device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, __nv_bfloat16* sVlof) {
+__device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, bool carry) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int q = warp & 3, jw = warp >> 2;  // lane quarter, and the warp's index among its 3 warps
   const int r = 32 * q + lane, a = r >> 1, i = r & 1;
@@ -589,22 +593,33 @@ __device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, _
     float v[32], w[32];
     tc::tmem_ld32x2(lane_addr + 32 * blk, lane_addr + 256 + 32 * blk, v, w);
 #pragma unroll
-    for (int k = 0; k < 32; ++k) v[k] += w[k];  // main + correction accumulators
-    if (!need) continue;
+    for (int k = 0; k < 32; ++k) {
+      v[k] += w[k];  // main + correction accumulators
+      w[k] = 0.f;    // carries
+    }
+    if (need) {
 #pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      const int b = b_lo + c;
-      if (b >= a && b <= up_hi) {
-        const int e = ku + 8 * b;
-        fold_scalar(sVf + e, sVlof + e, v[2 * c]);
-        fold_scalar(sVf + e + 2, sVlof + e + 2, v[2 * c + 1]);
-      } else if (b <= wrap_end) {
-        const int e = 8 * (b * na - (b * (b - 1)) / 2 - b) + kl;
-        fold_scalar(sVf + e, sVlof + e, sgn * v[2 * c]);
-        fold_scalar(sVf + e + 4, sVlof + e + 4, sgn * v[2 * c + 1]);
+      for (int c = 0; c < 16; ++c) {
+        const int b = b_lo + c;
+        if (b >= a && b <= up_hi) {
+          const int e = ku + 8 * b;
+          w[2 * c] = fold_carry(sVf + e, v[2 * c]);
+          w[2 * c + 1] = fold_carry(sVf + e + 2, v[2 * c + 1]);
+        } else if (b <= wrap_end) {
+          const int e = 8 * (b * na - (b * (b - 1)) / 2 - b) + kl;
+          w[2 * c] = sgn * fold_carry(sVf + e, sgn * v[2 * c]);
+          w[2 * c + 1] = sgn * fold_carry(sVf + e + 4, sgn * v[2 * c + 1]);
+        }
       }
     }
+    if (carry) {
+      uint32_t wb[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) wb[k] = __float_as_uint(w[k]);
+      tc::tmem_st32(lane_addr + 256 + 32 * blk, wb);
+    }
   }
+  if (carry) tc::tmem_wait_st();
 }
 
 // Source terms needed for a point source's J at (time t, channel ch).
@@ -669,8 +684,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   AntInfo<float>* sa = reinterpret_cast<AntInfo<float>*>(smem + S.off_ant);
   SrcInfo<float>* ss = reinterpret_cast<SrcInfo<float>*>(smem + S.off_src);
   Jones<float>* sV = reinterpret_cast<Jones<float>*>(smem + S.off_V);
-  __nv_bfloat16* sVlo16 = reinterpret_cast<__nv_bfloat16*>(smem + P.off_vlo16);  // tensor-core phase
-  Jones<float>* sVlo = reinterpret_cast<Jones<float>*>(smem + P.off_vlo32);      // extended sources
+  Jones<float>* sVlo = reinterpret_cast<Jones<float>*>(smem + P.off_vlo32);  // extended sources
   int* items = reinterpret_cast<int*>(smem + S.off_items);
   double* red = reinterpret_cast<double*>(smem + S.off_red);
   unsigned char* stage = smem + P.off_stage;
@@ -696,7 +710,6 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   __syncthreads();
   load_antennas(A, t, ch, sa);
   for (int i = tid; i < S.npairs; i += blockDim.x) sV[i] = jzero<float>();
-  for (int i = tid; i < S.npairs * 8; i += blockDim.x) sVlo16[i] = __float2bfloat16_rn(0.f);
   // the stage buffers' unused slots are read by the MMAs as zeros
   for (int i = tid; i < int(kTcStages * 2 * L::kMatBytes / 16); i += blockDim.x)
     reinterpret_cast<uint4*>(stage)[i] = make_uint4(0u, 0u, 0u, 0u);
@@ -770,7 +783,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
         if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1);
         tc::fence_after_thread_sync();
         bad = __any_sync(0xffffffffu, bad);  // the drain's TMEM loads are warp-collective
-        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), sVlo16);
+        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), g < nstages - 1);
         tc::fence_before_thread_sync();
         if (!bad) tc::mbar_arrive(accfree);
       }
@@ -794,14 +807,17 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
           tc::fence_after_thread_sync();
           const uint32_t hi = tc::smem_addr(stage + size_t(slot) * 2 * L::kMatBytes);
           const uint32_t lo = hi + L::kMatBytes;
-          const uint32_t acc0 = (first ? 0u : 1u);
+          // the main accumulators restart with every group; the correction
+          // accumulators only with the first stage (they carry the drains'
+          // rounding errors from group to group)
+          const uint32_t acc0 = (first ? 0u : 1u), cacc0 = (g == 0 ? 0u : 1u);
 #pragma unroll
           for (int kk = 0; kk < L::kKSteps; ++kk) {
             const uint32_t o = kk * L::kKStepBytes;
             const uint64_t ah = L::desc(hi + o), al = L::desc(lo + o);
-            const uint32_t acc = kk == 0 ? acc0 : 1u;
+            const uint32_t acc = kk == 0 ? acc0 : 1u, cacc = kk == 0 ? cacc0 : 1u;
             L::mma(tmem, ah, ah, idesc, acc);
-            L::mma(tmem + 256, ah, al, idesc, acc);
+            L::mma(tmem + 256, ah, al, idesc, cacc);
             L::mma(tmem + 256, al, ah, idesc, 1u);
           }
 #pragma unroll
@@ -809,10 +825,10 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
             const uint32_t oi = (kk + half) * L::kKStepBytes, orr = kk * L::kKStepBytes;
             const uint64_t ih = L::desc(hi + oi), il = L::desc(lo + oi);
             const uint64_t rh = L::desc(hi + orr), rl = L::desc(lo + orr);
-            const uint32_t acc = kk == 0 ? acc0 : 1u;
+            const uint32_t acc = kk == 0 ? acc0 : 1u, cacc = kk == 0 ? cacc0 : 1u;
             // D_im += A_im A_re^T
             L::mma(tmem + 128, ih, rh, idesc, acc);
-            L::mma(tmem + 384, ih, rl, idesc, acc);
+            L::mma(tmem + 384, ih, rl, idesc, cacc);
             L::mma(tmem + 384, il, rh, idesc, 1u);
             // D_im += (-A_re) A_im^T
             L::mma(tmem + 128, rh, ih, idesc_neg, 1u);
@@ -828,7 +844,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
         if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1);
         tc::fence_after_thread_sync();
         bad = __any_sync(0xffffffffu, bad);
-        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), sVlo16);
+        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), g < nstages - 1);
         tc::fence_before_thread_sync();
         if (!bad) tc::mbar_arrive(accfree);
       }
@@ -846,15 +862,10 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   const bool aborted = *abort_flag != 0;
 
   // ---- extended sources on the CUDA cores --------------------------------
-  // the tensor-core phase's BF16 low parts join the high parts; the
-  // extended sources accumulate with FP32 low parts in the stage region
+  // they accumulate with FP32 low parts in the stage region
   {
-    float* v = reinterpret_cast<float*>(sV);
     float* vlo = reinterpret_cast<float*>(sVlo);
-    for (int i = tid; i < S.npairs * 8; i += blockDim.x) {
-      v[i] += __bfloat162float(sVlo16[i]);
-      vlo[i] = 0.f;
-    }
+    for (int i = tid; i < S.npairs * 8; i += blockDim.x) vlo[i] = 0.f;
   }
   __syncthreads();
   const float kg = A.gauss_scale * f, ks = A.two_pi_over_c * f;
@@ -2116,8 +2127,7 @@ mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2,
   P.group = kTcGroup;
   // The stage region holds the operand stages during the tensor-core phase,
   // then the extended sources' Jones tile and the FP32 low parts of the pair
-  // accumulators; the BF16 low parts of the tensor-core phase have their own
-  // region.  All regions 128-byte aligned.
+  // accumulators.  All regions 128-byte aligned.
   const size_t row_bytes = mode == MB_MODE_SPLIT_TF32 ? TcGeom<MB_MODE_SPLIT_TF32>::kRowBytes
                                                       : TcGeom<MB_MODE_SPLIT_BF16>::kRowBytes;
   const size_t stage_bytes = size_t(kTcStages) * 2 * 128 * row_bytes;
@@ -2132,7 +2142,6 @@ mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2,
   S.off_ant = take(sizeof(AntInfo<float>) * A.na);
   S.off_src = take(sizeof(SrcInfo<float>) * S.st);
   S.off_V = take(vbytes);
-  P.off_vlo16 = take(size_t(S.npairs) * 8 * sizeof(__nv_bfloat16));
   S.off_items = take(sizeof(int) * (S.nitems + 128));
   S.off_red = take(sizeof(double) * 32);
   P.off_bar = take((2 * kTcStages + 3) * sizeof(uint64_t) + 16);
