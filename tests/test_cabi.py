@@ -104,3 +104,27 @@ def test_kernel_timing_without_launches():
     assert (ms.value, n.value) == (0.0, 0)
     st = _cabi.lib.mb_kernel_time(None, None, ctypes.byref(n))
     assert _cabi.STATUS_NAMES[st] == 'MB_ERR_NULL_PTR'
+
+
+def test_source_tile_options():
+    """Tile bits pass option validation (the call then stops at the short
+    workspace); unknown bits are rejected; the header and Python agree."""
+    from montblanc_gb300 import _cabi
+    text = open(HEADER).read()
+    assert re.search(r'#define MB_SOURCE_TILE_SHIFT 8\b', text)
+    assert _cabi.MB_SOURCE_TILE_MASK == 0x3 << 8
+    assert [_cabi.source_tile_bits(t) >> 8 for t in (0, 8, 16, 32)] == [0, 1, 2, 3]
+    with pytest.raises(ValueError):
+        _cabi.source_tile_bits(12)
+    d = _cabi.make_dims(2, 3, 3, 4, 2, beam=(2, 2, 2))
+    n = _cabi.lib.mb_rime_workspace_size(_cabi.MB_FLOAT32, 0, ctypes.byref(d), 0)
+    inp = _cabi.MbRimeInputs()
+    for name in _cabi.INPUT_NAMES:
+        setattr(inp, name, 256)
+    p = _cabi.make_props(gauss_scale=1, two_pi_over_c=1, sigma_sqrd=1, beam_ll=-1, beam_lm=-1,
+                         beam_lfreq=1, beam_ul=1, beam_um=1, beam_ufreq=2)
+    x2, fake = ctypes.c_void_p(256), ctypes.c_void_p(256)
+    for opts, want in ((_cabi.source_tile_bits(32), 'MB_ERR_WORKSPACE'), (1 << 12, 'MB_ERR_INVALID_ARG')):
+        st = _cabi.lib.mb_rime_forward(_cabi.MB_FLOAT32, 0, ctypes.byref(d), ctypes.byref(p), opts,
+                                       ctypes.byref(inp), None, None, x2, 0, fake, n - 1, None)
+        assert _cabi.STATUS_NAMES[st] == want, (opts, _cabi.STATUS_NAMES[st])
