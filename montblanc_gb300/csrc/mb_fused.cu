@@ -502,8 +502,10 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A,
 // from whichever of (a, b), (b, a) the cyclic rule in tc_drain picks.
 // Each operand value is split into hi + lo parts: the large hi.hi products
 // and the small hi.lo + lo.hi corrections accumulate in separate TMEM
-// accumulators (FP32), which are folded into float-float pair accumulators
-// in shared memory every kTcGroup stages.  The tensor core's FP32
+// accumulators (FP32).  Every kTcGroup stages their sum is folded into FP32
+// pair accumulators in shared memory, and the fold's rounding error goes
+// back into the correction accumulator (tc_drain), so pair and correction
+// accumulators together hold a float-float sum.  The tensor core's FP32
 // accumulation rounds toward zero, so its error grows with the number of
 // accumulations into one accumulator (about 2.5e-8 of the result per
 // accumulation for a coherent sum).  Measured on 20 000 point sources, each
