@@ -272,6 +272,29 @@ __device__ __forceinline__ void atomic_add_jones(Jones<T>* dst, const Jones<T>& 
   atomicAdd(d + 4, x.c.r); atomicAdd(d + 5, x.c.i); atomicAdd(d + 6, x.d.r); atomicAdd(d + 7, x.d.i);
 }
 
+// Adds the NV values of every active lane to acc[key * stride + j].  When
+// all active lanes of the warp share one key the warp sums first and one
+// lane adds; otherwise each active lane adds its own.  Every lane of the
+// warp calls it; key < 0 marks an inactive lane (its values must be 0).
+template <typename T, int NV>
+__device__ __forceinline__ void warp_keyed_add_stride(T* acc, int stride, int key, T (&v)[NV]) {
+  const unsigned full = 0xffffffffu;
+  const int k0 = __reduce_max_sync(full, key);
+  if (__all_sync(full, key < 0 || key == k0)) {
+    if (k0 < 0) return;
+#pragma unroll
+    for (int j = 0; j < NV; ++j)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(full, v[j], o);
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+      for (int j = 0; j < NV; ++j) atomicAdd(acc + k0 * stride + j, v[j]);
+  } else if (key >= 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) atomicAdd(acc + key * stride + j, v[j]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Epilogue (shared with the tensor-core path)
 // ---------------------------------------------------------------------------
@@ -286,56 +309,75 @@ __device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const J
   }
   __syncthreads();
   double part = 0.0;
-  for (int bl = threadIdx.x; bl < A.nbl; bl += blockDim.x) {
-    size_t tbl = size_t(t) * A.lnbl + bl;
-    int p = A.ant1[tbl], q = A.ant2[tbl];
-    size_t vidx = tbl * A.lchan + ch;
-    if (p < 0 || p >= A.na || q < 0 || q >= A.na) {  // invalid antenna index: NaN output
-      const T nan = T(NAN);
-      if (A.model_vis) jstore(A.model_vis + 8 * vidx, Jones<T>{{nan, nan}, {nan, nan}, {nan, nan}, {nan, nan}});
-      if (A.chi2 && !A.partial_out) A.chi2[vidx] = nan;
-      part += double(nan);
-      if (A.want_grad) jstore(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch), jzero<T>());
-      continue;
+  // Whole rounds of blockDim baselines, so that every lane of a warp takes
+  // part in the keyed warp sum of dchi^2/dG below.
+  const int rounds = (A.nbl + blockDim.x - 1) / blockDim.x;
+  for (int round = 0; round < rounds; ++round) {
+    const int bl = round * blockDim.x + threadIdx.x;
+    int key_p = -1;                  // antenna 1 of this lane's dchi^2/dG term (-1: none)
+    Jones<T> gp = jzero<T>();        // the term itself
+    if (bl < A.nbl) {
+      size_t tbl = size_t(t) * A.lnbl + bl;
+      int p = A.ant1[tbl], q = A.ant2[tbl];
+      size_t vidx = tbl * A.lchan + ch;
+      if (p < 0 || p >= A.na || q < 0 || q >= A.na) {  // invalid antenna index: NaN output
+        const T nan = T(NAN);
+        if (A.model_vis) jstore(A.model_vis + 8 * vidx, Jones<T>{{nan, nan}, {nan, nan}, {nan, nan}, {nan, nan}});
+        if (A.chi2 && !A.partial_out) A.chi2[vidx] = nan;
+        part += double(nan);
+        if (A.want_grad) jstore(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch), jzero<T>());
+      } else {
+        Jones<T> V = p <= q ? sV[pair_index(p, q, A.na)] : jherm(sV[pair_index(q, p, A.na)]);
+        if (A.accumulate_in) V = jadd(V, jload<T>(A.model_vis + 8 * vidx));
+        if (A.partial_out) {
+          jstore(A.model_vis + 8 * vidx, V);
+        } else {
+          const Jones<T> Gp = sG[p], Gq = sG[q];
+          Jones<T> M = jmulh(jmul(Gp, V), Gq);
+          Jones<T> O = jldg<T>(A.obs + 8 * vidx);
+          uchar4 fl = *reinterpret_cast<const uchar4*>(A.flag + 4 * vidx);
+          const uint8_t fv[4] = {fl.x, fl.y, fl.z, fl.w};
+          T w4[4] = {T(1), T(1), T(1), T(1)};
+          if (A.weights) {
+            for (int k = 0; k < 4; ++k) w4[k] = A.weight[4 * vidx + k];
+          }
+          Cx<T>* m4 = &M.a;
+          Cx<T>* o4 = &O.a;
+          Jones<T> R, gM;
+          Cx<T>* r4 = &R.a;
+          Cx<T>* g4 = &gM.a;
+          T term = T(0);
+          const T gscale = A.weights ? T(-2) : T(-2.0 * A.inv_sigma2);
+          for (int k = 0; k < 4; ++k) {
+            if (fv[k] > 0) { m4[k] = Cx<T>{T(0), T(0)}; o4[k] = Cx<T>{T(0), T(0)}; }
+            r4[k] = o4[k] - m4[k];
+            T re2 = r4[k].r * r4[k].r, im2 = r4[k].i * r4[k].i;
+            if (A.weights) { re2 *= w4[k]; im2 *= w4[k]; }
+            term += re2 + im2;
+            g4[k] = fv[k] > 0 ? Cx<T>{T(0), T(0)} : r4[k] * (gscale * w4[k]);
+          }
+          if (A.model_vis) jstore(A.model_vis + 8 * vidx, A.residuals ? R : M);
+          if (A.chi2) A.chi2[vidx] = term;
+          part += double(term);
+          if (A.want_grad) {
+            Jones<T> gV = jmul(jhmul(Gp, gM), Gq);
+            jstore(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch), gV);
+            key_p = p;
+            gp = jmul(gM, jmulh(Gq, V));
+            // antenna 2 differs from lane to lane (consecutive baselines)
+            atomic_add_jones(&sdG[q], jmul(jherm(gM), jmul(Gp, V)));
+          }
+        }
+      }
     }
-    Jones<T> V = p <= q ? sV[pair_index(p, q, A.na)] : jherm(sV[pair_index(q, p, A.na)]);
-    if (A.accumulate_in) V = jadd(V, jload<T>(A.model_vis + 8 * vidx));
-    if (A.partial_out) {
-      jstore(A.model_vis + 8 * vidx, V);
-      continue;
-    }
-    const Jones<T> Gp = sG[p], Gq = sG[q];
-    Jones<T> M = jmulh(jmul(Gp, V), Gq);
-    Jones<T> O = jldg<T>(A.obs + 8 * vidx);
-    uchar4 fl = *reinterpret_cast<const uchar4*>(A.flag + 4 * vidx);
-    const uint8_t fv[4] = {fl.x, fl.y, fl.z, fl.w};
-    T w4[4] = {T(1), T(1), T(1), T(1)};
-    if (A.weights) {
-      for (int k = 0; k < 4; ++k) w4[k] = A.weight[4 * vidx + k];
-    }
-    Cx<T>* m4 = &M.a;
-    Cx<T>* o4 = &O.a;
-    Jones<T> R, gM;
-    Cx<T>* r4 = &R.a;
-    Cx<T>* g4 = &gM.a;
-    T term = T(0);
-    const T gscale = A.weights ? T(-2) : T(-2.0 * A.inv_sigma2);
-    for (int k = 0; k < 4; ++k) {
-      if (fv[k] > 0) { m4[k] = Cx<T>{T(0), T(0)}; o4[k] = Cx<T>{T(0), T(0)}; }
-      r4[k] = o4[k] - m4[k];
-      T re2 = r4[k].r * r4[k].r, im2 = r4[k].i * r4[k].i;
-      if (A.weights) { re2 *= w4[k]; im2 *= w4[k]; }
-      term += re2 + im2;
-      g4[k] = fv[k] > 0 ? Cx<T>{T(0), T(0)} : r4[k] * (gscale * w4[k]);
-    }
-    if (A.model_vis) jstore(A.model_vis + 8 * vidx, A.residuals ? R : M);
-    if (A.chi2) A.chi2[vidx] = term;
-    part += double(term);
-    if (A.want_grad) {
-      Jones<T> gV = jmul(jhmul(Gp, gM), Gq);
-      jstore(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch), gV);
-      atomic_add_jones(&sdG[p], jmul(gM, jmulh(Gq, V)));
-      atomic_add_jones(&sdG[q], jmul(jherm(gM), jmul(Gp, V)));
+    // antenna 1 is mostly shared by the warp's consecutive baselines: sum
+    // over the warp first, then one lane adds
+    if (A.want_grad && !A.partial_out) {
+      T* gv = reinterpret_cast<T*>(&gp);
+      T v8[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v8[k] = gv[k];
+      warp_keyed_add_stride<T, 8>(reinterpret_cast<T*>(sdG), 8, key_p, v8);
     }
   }
   double tot = block_sum<T>(part, red);
@@ -1169,27 +1211,11 @@ __device__ void adj_consume_point(const FusedArgs<T>& A, const SmemPlan& S, int 
   }
 }
 
-// Adds the NV values of every active lane to acc[key * kNAcc + first + j].
-// When all active lanes of the warp share one key the warp sums first and
-// one lane adds; otherwise each active lane adds its own.  Every lane of the
-// warp calls it; key < 0 marks an inactive lane (its values must be 0).
+// Adds the NV values of every active lane to acc[key * kNAcc + first + j]
+// (warp_keyed_add_stride with the per-source accumulator stride).
 template <typename T, int NV>
 __device__ __forceinline__ void warp_keyed_add(T* acc, int first, int key, T (&v)[NV]) {
-  const unsigned full = 0xffffffffu;
-  const int k0 = __reduce_max_sync(full, key);
-  if (__all_sync(full, key < 0 || key == k0)) {
-    if (k0 < 0) return;
-#pragma unroll
-    for (int j = 0; j < NV; ++j)
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(full, v[j], o);
-    if ((threadIdx.x & 31) == 0)
-#pragma unroll
-      for (int j = 0; j < NV; ++j) atomicAdd(acc + k0 * kNAcc + first + j, v[j]);
-  } else if (key >= 0) {
-#pragma unroll
-    for (int j = 0; j < NV; ++j) atomicAdd(acc + key * kNAcc + first + j, v[j]);
-  }
+  warp_keyed_add_stride<T, NV>(acc + first, kNAcc, key, v);
 }
 
 // Chain d chi^2 / dJ(s, a) through E and K: d chi^2 / d(l, m) of the item
