@@ -134,14 +134,21 @@ def terms_of(name):
 # distributed plumbing
 # ---------------------------------------------------------------------------
 def dist_init(n):
+    """(world size, rank, local rank) from the launcher's environment; with
+    more than one rank, a process group over NCCL (one GPU per rank), or
+    over gloo where no GPU is visible (host-side tests of the replica
+    plumbing)."""
     import torch
     ws = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     local = int(os.environ.get('LOCAL_RANK', '0'))
     if ws > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+        else:
+            dist.init_process_group('gloo')
     elif torch.cuda.is_available():
         torch.cuda.set_device(0)
     return ws, rank, local
@@ -154,13 +161,21 @@ def barrier(ws):
 
 
 def max_over_ranks(ws, x):
+    """The largest x over the ranks (the slowest replica's time)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device='cuda')
+    dev = 'cuda' if dist.get_backend() == 'nccl' else 'cpu'
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_value(ws, terms_per_rank, ms_max):
+    """Whole-job throughput of ws replicas that each process terms_per_rank
+    terms per step, timed by the slowest rank (weak scaling)."""
+    return ws * terms_per_rank / (ms_max * 1e-3)
 
 
 # ---------------------------------------------------------------------------
@@ -542,7 +557,7 @@ def main():
     ms, fwd_ms, adj_ms = time_resident(prob, args.mode, args.steps, args.warmup, ws, kernels)
     clk = clocks.stop()
     ms_max = max_over_ranks(ws, ms)
-    value = ws * terms / (ms_max * 1e-3)
+    value = whole_job_value(ws, terms, ms_max)
 
     plain = None
     if not args.no_plain and args.mode != 'native':
