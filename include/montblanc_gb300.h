@@ -239,6 +239,13 @@ mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
 mb_status mb_tc_selftest(const float* A, const float* B, int K, int mode,
                          float* D, int* status, void* stream);
 
+/* Diagnostic, no counterpart in the reference: the bounded-wait path of the
+ * tensor-core kernels on a wait that cannot complete.  One CTA allocates
+ * TMEM, waits at most poll_limit polls on an mbarrier that nothing arrives
+ * on, sets *status (device int) to 1 when the wait gives up, frees TMEM and
+ * returns.  Stream-ordered, no host synchronisation. */
+mb_status mb_wait_selftest(uint32_t poll_limit, int* status, void* stream);
+
 /* Diagnostics, no counterpart in the reference: launch accounting and
  * per-kernel CUDA-event timing of this library's kernels.
  * mb_kernel_launches: kernels launched by the library in this process.

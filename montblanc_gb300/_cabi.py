@@ -93,6 +93,7 @@ SIGNATURES = {
     'mb_rime_adjoint': (_i32, [_i32, _i32, _pdims, _pprops, _u32, ctypes.POINTER(MbRimeInputs), _dbl,
                                ctypes.POINTER(MbRimeGrads), _vp, _sz, _vp]),
     'mb_tc_selftest': (_i32, [_vp, _vp, _i32, _i32, _vp, _vp, _vp]),
+    'mb_wait_selftest': (_i32, [_u32, _vp, _vp]),
     'mb_rime_noalloc_max_units': (_sz, []),
     'mb_rime_forward_noalloc': (_i32, [_i32, _pdims, _pprops, _u32, ctypes.POINTER(MbRimeInputs), _vp, _vp,
                                        _vp, _vp]),

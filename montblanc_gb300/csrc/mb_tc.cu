@@ -156,6 +156,27 @@ __global__ void __launch_bounds__(160) tc_selftest_ta_kernel(const float* __rest
   if (threadIdx.x == 0 && abort_flag) *status = 1;
 }
 
+// A wait that cannot complete: the mbarrier's phase 0 needs one arrival and
+// none comes, so the bounded wait gives up after `limit` polls; the kernel
+// records it and frees its TMEM like the fused kernels' abort path.
+__global__ void wait_selftest_kernel(uint32_t limit, int* status) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_slot;
+  const int warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
+  tc::fence_proxy_async_smem();
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, 32);
+  tc::fence_before_thread_sync();
+  __syncthreads();
+  tc::fence_after_thread_sync();
+  const bool ok = warp == 0 ? tc::mbar_wait(&bar, 0, limit) : true;
+  if (!ok && threadIdx.x == 0) *status = 1;
+  tc::fence_before_thread_sync();
+  __syncthreads();
+  tc::fence_after_thread_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem_slot, 32);
+}
+
 }  // namespace
 
 }  // namespace mb
@@ -196,6 +217,16 @@ mb_status mb_tc_selftest(const float* A, const float* B, int K, int mode, float*
     return fail(MB_ERR_INVALID_ARG, "mode must be a split-precision mode");
   }
   return check_launch("tc_selftest_kernel");
+}
+
+mb_status mb_wait_selftest(uint32_t poll_limit, int* status, void* stream) {
+  MB_REQUIRE(status, "status");
+  cudaStream_t s = as_stream(stream);
+  {
+    KernelScope ks_("wait_selftest_kernel", s);
+    wait_selftest_kernel<<<1, 64, 0, s>>>(poll_limit, status);
+  }
+  return check_launch("wait_selftest_kernel");
 }
 
 }  // extern "C"

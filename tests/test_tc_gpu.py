@@ -110,3 +110,28 @@ def test_split_forward_many_sources_against_fp64(mode):
     err_native = np.linalg.norm(c - b) / np.linalg.norm(b)
     assert err < (2e-6 if mode == 'split_tf32' else 5e-5), (err, err_native)
     assert abs(x32 - x64) <= 1e-3 * abs(x64)
+
+
+@pytest.mark.parametrize('limit', [0, 1 << 10])
+def test_bounded_wait_gives_up_and_the_context_stays_usable(limit):
+    """A wait on an mbarrier that nothing arrives on gives up after its poll
+    limit, reports it, frees its TMEM; the tensor-core kernels run
+    correctly right after it."""
+    import torch
+    from montblanc_gb300 import _cabi
+    status = torch.zeros(1, dtype=torch.int32, device='cuda')
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _cabi.call('mb_wait_selftest', limit, status.data_ptr(), stream)
+    torch.cuda.synchronize()
+    assert status.item() == 1
+    g = torch.Generator(device='cpu').manual_seed(3)
+    A = torch.randn(128, 64, generator=g).cuda()
+    B = torch.randn(128, 64, generator=g).cuda()
+    D = torch.zeros(128, 128, dtype=torch.float32, device='cuda')
+    status.zero_()
+    _cabi.call('mb_tc_selftest', A.data_ptr(), B.data_ptr(), 64, _cabi.MODES['split_tf32'], D.data_ptr(),
+               status.data_ptr(), stream)
+    torch.cuda.synchronize()
+    assert status.item() == 0
+    ref = (A.double() @ B.double().T)
+    assert float((D.double() - ref).abs().max() / ref.abs().max()) < 5e-6
