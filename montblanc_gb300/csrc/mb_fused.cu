@@ -2146,35 +2146,42 @@ mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2,
   if (A.na > 64)
     return fail(MB_ERR_UNSUPPORTED, "split-precision modes handle up to 64 antennas (got %d)", A.na);
   const int units = A.ntime * A.nchan;
-  SmemPlan S = make_plan<float>(A.na, false, false);
-  // The tensor-core kernel runs with kTcThreads threads; its extended-source
-  // phase uses the same pair-tile plan with that thread count.
-  S.nthreads = kTcThreads;
-  S.groups = S.nitems <= kTcThreads ? std::min(8, std::max(1, kTcThreads / S.nitems)) : 1;
-  TcPlan P;
-  P.group = kTcGroup;
   // The stage region holds the operand stages during the tensor-core phase,
   // then the extended sources' Jones tile and the FP32 low parts of the pair
-  // accumulators.  All regions 128-byte aligned.
+  // accumulators.  All regions 128-byte aligned.  The extended sources take
+  // 32-source tiles (fewer tile passes and barriers; 35.1 -> 24.6 ms on the
+  // 100 x 27 x 64 mixed workload) unless the source-tile option asks
+  // otherwise or the layout does not fit, then 16 or 8.
   const size_t row_bytes = mode == MB_MODE_SPLIT_TF32 ? TcGeom<MB_MODE_SPLIT_TF32>::kRowBytes
                                                       : TcGeom<MB_MODE_SPLIT_BF16>::kRowBytes;
   const size_t stage_bytes = size_t(kTcStages) * 2 * 128 * row_bytes;
-  const size_t jbytes = align_up(size_t(S.jrow) * S.st, 128);
-  const size_t vbytes = sizeof(Jones<float>) * S.npairs;
-  size_t o = 0;
-  auto take = [&o](size_t b) { size_t r = o; o = align_up(o + b, 128); return r; };
-  P.off_stage = take(std::max(stage_bytes, jbytes + vbytes));
-  P.off_vlo32 = P.off_stage + jbytes;
-  S.off_J = P.off_stage;
-  S.off_Vlo = P.off_vlo32;
-  S.off_ant = take(sizeof(AntInfo<float>) * A.na);
-  S.off_src = take(sizeof(SrcInfo<float>) * S.st);
-  S.off_V = take(vbytes);
-  S.off_items = take(sizeof(int) * (S.nitems + 128));
-  S.off_red = take(sizeof(double) * 32);
-  P.off_bar = take((2 * kTcStages + 3) * sizeof(uint64_t) + 16);
-  P.total = o;
-  if (P.total > 227 * 1024)
+  SmemPlan S;
+  TcPlan P;
+  for (int tile = A.src_tile ? A.src_tile : 32;; tile /= 2) {
+    S = make_plan<float>(A.na, false, false, tile);
+    // The tensor-core kernel runs with kTcThreads threads; its extended-source
+    // phase uses the same pair-tile plan with that thread count.
+    S.nthreads = kTcThreads;
+    S.groups = S.nitems <= kTcThreads ? std::min(8, std::max(1, kTcThreads / S.nitems)) : 1;
+    P.group = kTcGroup;
+    const size_t jbytes = align_up(size_t(S.jrow) * S.st, 128);
+    const size_t vbytes = sizeof(Jones<float>) * S.npairs;
+    size_t o = 0;
+    auto take = [&o](size_t b) { size_t r = o; o = align_up(o + b, 128); return r; };
+    P.off_stage = take(std::max(stage_bytes, jbytes + vbytes));
+    P.off_vlo32 = P.off_stage + jbytes;
+    S.off_J = P.off_stage;
+    S.off_Vlo = P.off_vlo32;
+    S.off_ant = take(sizeof(AntInfo<float>) * A.na);
+    S.off_src = take(sizeof(SrcInfo<float>) * S.st);
+    S.off_V = take(vbytes);
+    S.off_items = take(sizeof(int) * (S.nitems + 128));
+    S.off_red = take(sizeof(double) * 32);
+    P.off_bar = take((2 * kTcStages + 3) * sizeof(uint64_t) + 16);
+    P.total = o;
+    if (P.total <= kMaxDynamicSmem || tile <= 8) break;
+  }
+  if (P.total > kMaxDynamicSmem)
     return fail(MB_ERR_UNSUPPORTED, "split-precision kernel needs %zu bytes of shared memory for na=%d",
                 P.total, A.na);
   if (A.err) MB_CUDA(cudaMemsetAsync(A.err, 0, sizeof(int), stream));
