@@ -20,7 +20,6 @@ collective, so the job total is N * terms / (max over ranks of the time).
 Prints one JSON line (rank 0).
 """
 import argparse
-import ctypes
 import json
 import math
 import os

@@ -1,8 +1,4 @@
 """Helpers for the GPU parity tests: build solvers / problems from fixtures."""
-import numpy as np
-
-import golden_io
-
 SOLVER_ARRAYS = ('uvw', 'antenna1', 'antenna2', 'frequency', 'ref_frequency', 'parallactic_angles',
                  'point_errors', 'antenna_scaling', 'E_beam', 'G_term', 'lm', 'stokes', 'alpha',
                  'gauss_shape', 'sersic_shape', 'flag', 'weight_vector', 'observed_vis')
