@@ -158,9 +158,8 @@ def test_factory_requires_msfile():
 @pytest.mark.gpu
 @pytest.mark.parametrize('version', ['v4', 'v5'])
 def test_solver_from_measurement_set(version):
-    """rime_solver(data_source='ms') sizes the solver from the MeasurementSet
-    and holds its arrays; its chi^2 equals that of a solver given the same
-    arrays by hand."""
+    """rime_solver(data_source='ms') sizes the solver from the MeasurementSet,
+    holds the loader's arrays (cast to the solver's dtypes) and solves."""
     import montblanc_gb300 as mb
     tables, _ = _ms()
     cfg = mb.rime_solver_cfg(data_source='ms', msfile=tables, sources=mb.sources(point=3, gaussian=1),
@@ -177,3 +176,49 @@ def test_solver_from_measurement_set(version):
         np.testing.assert_array_equal(g, A[name].astype(g.dtype))
     s.solve()
     assert np.isfinite(s.X2)
+
+
+def test_path_branch_with_a_casacore_stand_in(monkeypatch):
+    """A MeasurementSet path goes through casacore.tables: table(path) for
+    MAIN and table('path::NAME') for each sub-table, opened read-only, then
+    colnames / getcol / nrows / close.  A stand-in module serves the
+    in-memory tables under those names."""
+    import sys
+    import types
+    tables, truth = _ms()
+    opened, closed = [], []
+
+    class Table(object):
+        def __init__(self, path, ack=True, readonly=False):
+            assert ack is False and readonly is True
+            name = path.split('::')[1] if '::' in path else 'MAIN'
+            assert path.split('::')[0] == '/data/obs.ms'
+            self.cols = tables[name]
+            opened.append(name)
+
+        def colnames(self):
+            return list(self.cols)
+
+        def getcol(self, name):
+            return self.cols[name]
+
+        def nrows(self):
+            return len(next(iter(self.cols.values())))
+
+        def close(self):
+            closed.append(1)
+
+    mod = types.ModuleType('casacore.tables')
+    mod.table = Table
+    pkg = types.ModuleType('casacore')
+    pkg.tables = mod
+    monkeypatch.setitem(sys.modules, 'casacore', pkg)
+    monkeypatch.setitem(sys.modules, 'casacore.tables', mod)
+    with ms.MeasurementSetLoader('/data/obs.ms') as L:
+        assert L.get_dims() == (NTIME, NA * (NA - 1) // 2, NA, 2, 2 * CPB)
+        A = L.arrays(init_weights='weight')
+    assert sorted(opened) == sorted(['MAIN'] + list(ms.SUBTABLES))
+    assert len(closed) == len(opened)
+    B = ms.MeasurementSetLoader(tables).arrays(init_weights='weight')
+    for k in B:
+        np.testing.assert_array_equal(A[k], B[k])
