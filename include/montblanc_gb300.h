@@ -14,7 +14,8 @@
  * failure, sets a thread-local message readable with mb_last_error_string().
  * No entry point allocates device memory; scratch space is reported by the
  * *_workspace_size functions and passed in by the caller.  Launches are
- * asynchronous on the given stream; no entry point synchronises the host.
+ * asynchronous on the given stream; only the status and timing queries
+ * (mb_rime_status, mb_kernel_time) synchronise the host.
  */
 #ifndef MONTBLANC_GB300_H
 #define MONTBLANC_GB300_H
@@ -228,6 +229,28 @@ mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
                           const mb_rime_grads* grads, void* workspace,
                           size_t workspace_bytes, void* stream);
 
+/* Device-side status of the last mb_rime_forward (and the mb_rime_adjoint
+ * calls after it) that used this workspace, with the same dtype, mode, dims
+ * and want_grad as the forward.  The tensor-core kernels' waits are bounded:
+ * a wait that gives up makes the kernel skip its remaining work and record
+ * MB_ERR_TIMEOUT in the workspace; the chi^2 of such a call is NaN.  This
+ * synchronises `stream`, reads that record and returns MB_ERR_TIMEOUT if it
+ * is set, MB_OK otherwise.  (The launches themselves return before the
+ * kernels run, so they cannot report it.)  Replaces the error surfacing of
+ * the blocking .get() in RimeSumCoherencies.py:531-536. */
+mb_status mb_rime_status(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
+                         int want_grad, const void* workspace,
+                         size_t workspace_bytes, void* stream);
+
+/* Diagnostic, no counterpart in the reference: the poll limit of the
+ * pipeline waits of the tensor-core kernels on the current device (default
+ * mb_default_wait_limit() = 2^20).  0 makes every such wait give up at once,
+ * which exercises the MB_ERR_TIMEOUT path without a fault: the kernels still
+ * wait, with the default limit, for the MMAs they issued before freeing
+ * tensor memory.  Synchronous. */
+mb_status mb_set_wait_limit(uint32_t polls);
+uint32_t mb_default_wait_limit(void);
+
 /* Diagnostic, no counterpart in the reference: D (128 x 128, row-major) =
  * A (128 x K) . B (128 x K)^T for row-major FP32 device arrays, computed
  * with the split-precision tensor-core operand path of the fused kernels
@@ -272,14 +295,19 @@ const char* mb_kernel_timing_name(int i);
  * synchronise the device.  Such callers cannot size and pass the workspace
  * mb_rime_forward needs.
  *
- * Same inputs, outputs and results as mb_rime_forward in MB_MODE_NATIVE
- * with want_grad = 0.  Its only scratch (one FP64 partial sum per (time,
- * channel) unit) is a static device array inside the library: at most
- * mb_rime_noalloc_max_units() = 131072 units (ntime * nchan active
- * extents); larger requests return MB_ERR_UNSUPPORTED.  The array costs
- * 1 MiB on every GPU that loads the library, for the life of the process.
- * The first call on a device looks the array's device address up
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Same inputs and outputs as mb_rime_forward in MB_MODE_NATIVE with
+ * want_grad = 0, and the same results up to rounding: in FP32 the beam is
+ * interpolated from the cube and sqrt(B) formed in the kernel (no per-call
+ * tables), so results differ from mb_rime_forward's in the last bits.  Its
+ * only scratch (one FP64 partial sum per (time, channel) unit) is a static
+ * device array inside the library: at most mb_rime_noalloc_max_units() =
+ * 131072 units (ntime * nchan active extents); larger requests return
+ * MB_ERR_UNSUPPORTED.  The array costs 1 MiB on every GPU that loads the
+ * library, for the life of the process.  Each call outside stream capture
+ * looks the array's device address up (cudaGetSymbolAddress, no
+ * allocation); a call during capture uses the address the last uncaptured
+ * call on that device found, so make one call on each device before
+ * capturing, and one after a cudaDeviceReset before capturing again.
  * All calls share the array: calls whose kernels may run at the same time
  * (on unordered streams) race on it and must be serialised by the caller.
  * It allocates nothing: no cudaMalloc, cudaFree or allocating library call.

@@ -92,6 +92,9 @@ SIGNATURES = {
                                _vp, _vp, _i32, _vp, _sz, _vp]),
     'mb_rime_adjoint': (_i32, [_i32, _i32, _pdims, _pprops, _u32, ctypes.POINTER(MbRimeInputs), _dbl,
                                ctypes.POINTER(MbRimeGrads), _vp, _sz, _vp]),
+    'mb_rime_status': (_i32, [_i32, _i32, _pdims, _i32, _vp, _sz, _vp]),
+    'mb_set_wait_limit': (_i32, [_u32]),
+    'mb_default_wait_limit': (_u32, []),
     'mb_tc_selftest': (_i32, [_vp, _vp, _i32, _i32, _vp, _vp, _vp]),
     'mb_wait_selftest': (_i32, [_u32, _vp, _vp]),
     'mb_rime_noalloc_max_units': (_sz, []),

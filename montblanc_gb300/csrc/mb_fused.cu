@@ -29,6 +29,14 @@
 
 namespace mb {
 
+// Poll limit of the pipeline waits (producer <-> MMA <-> drain) in the
+// tensor-core kernels, per device.  A wait that runs out marks the CTA bad;
+// the CTA then skips its remaining work, still waits (with the fixed limit
+// of tc::mbar_wait) for every MMA it issued, frees its TMEM, and writes
+// MB_ERR_TIMEOUT into the workspace's error word (read back by
+// mb_rime_status).  mb_set_wait_limit changes it for tests of that path.
+__device__ uint32_t g_pipe_wait_limit = 1u << 20;
+
 __global__ void sum_partials_kernel(const double* __restrict__ partial, int n, double scale,
                                     double* __restrict__ out);
 
@@ -783,6 +791,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   const int nstages = (A.npsrc + NSRC - 1) / NSRC;
   const int group = P.group;
   const float log2_ratio = log2f(f / A.ref_freq[ch]);
+  const uint32_t wlim = g_pipe_wait_limit;
   bool bad = false;
 
   if (warp < kTcProducerWarps) {
@@ -799,7 +808,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
     // the MMA warp's waits then give up too, and everyone reaches the end.
     for (int g = 0; g < nstages; ++g) {
       const int slot = g % kTcStages, use = g / kTcStages;
-      if (!bad) bad = !tc::mbar_wait(empty + slot, (use & 1) ^ 1);
+      if (!bad) bad = !tc::mbar_wait(empty + slot, (use & 1) ^ 1, wlim);
       if (!bad) {
         const int s0 = g * NSRC, ns = min(NSRC, A.npsrc - s0);
         unsigned char* hi = stage + size_t(slot) * 2 * L::kMatBytes;
@@ -824,7 +833,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
         tc::mbar_arrive(full + slot);
       }
       if ((g % group) == group - 1 || g == nstages - 1) {
-        if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1);
+        if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1, wlim);
         tc::fence_after_thread_sync();
         bad = __any_sync(0xffffffffu, bad);  // the drain's TMEM loads are warp-collective
         if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), g < nstages - 1);
@@ -843,10 +852,10 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
       const bool first = (g % group) == 0, last = (g % group) == group - 1 || g == nstages - 1;
       if (lane == 0 && !bad) {
         if (first && g > 0) {
-          bad = !tc::mbar_wait(accfree, ((g / group) - 1) & 1);
+          bad = !tc::mbar_wait(accfree, ((g / group) - 1) & 1, wlim);
           tc::fence_after_thread_sync();
         }
-        if (!bad) bad = !tc::mbar_wait(full + slot, use & 1);
+        if (!bad) bad = !tc::mbar_wait(full + slot, use & 1, wlim);
         if (!bad) {
           tc::fence_after_thread_sync();
           const uint32_t hi = tc::smem_addr(stage + size_t(slot) * 2 * L::kMatBytes);
@@ -885,7 +894,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
         }
       }
       if (last) {
-        if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1);
+        if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1, wlim);
         tc::fence_after_thread_sync();
         bad = __any_sync(0xffffffffu, bad);
         if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), g < nstages - 1);
@@ -1683,6 +1692,7 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
   const float half_log_ratio = 0.5f * logf(f / A.ref_freq[ch]);
   const float dphase = float(2.0 * kPi * nu_over_c);
   const int ntiles = (A.npsrc + kTaKappa - 1) / kTaKappa;
+  const uint32_t wlim = g_pipe_wait_limit;
   // Units start their tile sweep at different tiles, so that the CTAs in
   // flight (neighbouring channels) do not update the same sources' FP64
   // accumulators at the same time.
@@ -1785,10 +1795,10 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
         issued = true;
       }
       // ---- dJ of the tile: TMEM buffer grp ------------------------------
-      if (!bad) bad = !tc::mbar_wait(dfull + grp, k & 1);
+      if (!bad) bad = !tc::mbar_wait(dfull + grp, k & 1, wlim);
       tc::fence_after_thread_sync();
       float v[32];  // v[2s + kc] = Re dJ(s)[i][kc], v[16 + 2s + kc] = Im
-      {
+      if (!__any_sync(0xffffffffu, bad)) {  // warp-collective loads, only of finished MMAs
         float re[32], im[32];
         tc::tmem_ld32(tlane, re);
         tc::tmem_ld32(tlane + 32, im);
@@ -1797,6 +1807,10 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
           v[e] = re[e] + re[16 + e];
           v[16 + e] = im[e] + im[16 + e];
         }
+      } else {
+        bad = true;
+#pragma unroll
+        for (int e = 0; e < 32; ++e) v[e] = 0.f;
       }
       // own row i of dJ for sources 4i + u; the partner lane (a, 1 - i)
       // holds row 1 - i.  Give it row i of its sources 4(1 - i) + u.
@@ -2184,7 +2198,6 @@ mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2,
   if (P.total > kMaxDynamicSmem)
     return fail(MB_ERR_UNSUPPORTED, "split-precision kernel needs %zu bytes of shared memory for na=%d",
                 P.total, A.na);
-  if (A.err) MB_CUDA(cudaMemsetAsync(A.err, 0, sizeof(int), stream));
   if (mode == MB_MODE_SPLIT_TF32) {
     auto kern = coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
@@ -2206,6 +2219,7 @@ template <typename T>
 mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* ws, const WsLayout& L,
                          cudaStream_t stream) {
   const int units = A.ntime * A.nchan;
+  if (A.err) MB_CUDA(cudaMemsetAsync(A.err, 0, sizeof(int), stream));
   if (units == 0) {
     MB_CUDA(cudaMemsetAsync(X2, 0, sizeof(double), stream));
     return MB_OK;
@@ -2239,7 +2253,8 @@ mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
     return fail(MB_ERR_UNSUPPORTED, "split-precision modes handle up to 64 antennas (got %d)", A.na);
   if (A.yop == nullptr) return fail(MB_ERR_WORKSPACE, "workspace lacks the adjoint operand region");
   const int units = A.ntime * A.nchan;
-  if (A.err) MB_CUDA(cudaMemsetAsync(A.err, 0, sizeof(int), stream));
+  // the error word is the forward's (cleared there): an adjoint after a
+  // forward whose waits gave up does no work and keeps reporting it
   if (A.npsrc > 0) {
     const size_t ysmem = size_t(A.na) * A.na * sizeof(Jones<float>);
     MB_CUDA(cudaFuncSetAttribute(yop_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(ysmem)));
@@ -2335,13 +2350,20 @@ static double* g_noalloc_ptr[kMaxDevices] = {};
 
 // Device address of g_noalloc_partials on the current device.  In host code
 // the symbol names a host-side stand-in, so the address is looked up with
-// cudaGetSymbolAddress once per device (with that device current) and cached.
-mb_status noalloc_scratch(double** out) {
+// cudaGetSymbolAddress (with the device current).  Outside stream capture it
+// is looked up on every call (cheap, and still right after a
+// cudaDeviceReset reloaded the module); during capture the address of the
+// last uncaptured call on the device is used.
+mb_status noalloc_scratch(double** out, cudaStream_t stream) {
   int dev = 0;
   MB_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(MB_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  MB_CUDA(cudaStreamIsCapturing(stream, &cap));
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (g_noalloc_ptr[dev] == nullptr) {
+  if (cap == cudaStreamCaptureStatusNone || g_noalloc_ptr[dev] == nullptr) {
+    if (cap != cudaStreamCaptureStatusNone)
+      return fail(MB_ERR_INVALID_ARG, "mb_rime_forward_noalloc: call it once on this device before stream capture");
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
     if (e != cudaSuccess)
@@ -2445,6 +2467,34 @@ mb_status mb_rime_adjoint(mb_dtype dtype, mb_mode mode, const mb_dims* dims, con
   return launch_adjoint(A, mode, grad_scale, grads, workspace, L, s);
 }
 
+mb_status mb_rime_status(mb_dtype dtype, mb_mode mode, const mb_dims* dims, int want_grad, const void* workspace,
+                         size_t workspace_bytes, void* stream) {
+  MB_CHECK(check_dims(dims, true));
+  if (dtype != MB_FLOAT32 && dtype != MB_FLOAT64) return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
+  WsLayout L = ws_layout(dtype, mode, dims, want_grad != 0);
+  if (workspace == nullptr || workspace_bytes < L.total || (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return fail(MB_ERR_WORKSPACE, "workspace must be >= %zu bytes and 256-byte aligned (got %zu)", L.total,
+                workspace_bytes);
+  cudaStream_t s = as_stream(stream);
+  int word = 0;
+  MB_CUDA(cudaMemcpyAsync(&word, static_cast<const char*>(workspace) + L.err, sizeof(int), cudaMemcpyDeviceToHost,
+                          s));
+  MB_CUDA(cudaStreamSynchronize(s));
+  if (word == int(MB_ERR_TIMEOUT))
+    return fail(MB_ERR_TIMEOUT,
+                "a bounded wait of the tensor-core kernels gave up: chi^2, model visibilities and gradients of "
+                "this call are invalid");
+  if (word != 0) return fail(MB_ERR_CUDA, "unexpected device error word %d", word);
+  return MB_OK;
+}
+
+mb_status mb_set_wait_limit(uint32_t polls) {
+  MB_CUDA(cudaMemcpyToSymbol(g_pipe_wait_limit, &polls, sizeof(polls)));
+  return MB_OK;
+}
+
+uint32_t mb_default_wait_limit(void) { return 1u << 20; }
+
 }  // extern "C"
 
 extern "C" {
@@ -2463,9 +2513,9 @@ mb_status mb_rime_forward_noalloc(mb_dtype dtype, const mb_dims* dims, const mb_
                 "mb_rime_forward_noalloc handles at most %zu (time, channel) units (got %zu = %u x %u); "
                 "split the call over time or use mb_rime_forward with a workspace",
                 kNoallocMaxUnits, units, ext(dims->ntime), ext(dims->nchan));
-  double* partials = nullptr;
-  MB_CHECK(noalloc_scratch(&partials));
   cudaStream_t s = as_stream(stream);
+  double* partials = nullptr;
+  MB_CHECK(noalloc_scratch(&partials, s));
   WsLayout L = ws_layout(dtype, MB_MODE_NATIVE, dims, false);
   if (dtype == MB_FLOAT32) {
     FusedArgs<float> A;

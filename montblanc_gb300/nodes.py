@@ -189,6 +189,10 @@ class RimeV4Fused(Node):
                    ptr(self._x2), 0, ptr(ws), ws.numel(), _stream(s, stream))
         if d.nsrc.upper_extent < d.nsrc.global_size:
             return
+        # reads chi^2 back (a host synchronisation, like the reference's
+        # .get()), after checking that no bounded device wait gave up
+        _cabi.call('mb_rime_status', s.mb_dtype(), mode, ctypes.byref(d), 0, ptr(ws), ws.numel(),
+                   _stream(s, stream))
         s.set_X2(self._x2.item())
 
     def post_execution(self, solver, stream=None):

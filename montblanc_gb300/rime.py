@@ -166,6 +166,15 @@ class RimeProblem(object):
         g = self.adjoint(mode=mode, stream=stream)
         return x2, g
 
+    def check(self, mode='native', want_grad=False, stream=None):
+        """Synchronise and raise MontblancError (MB_ERR_TIMEOUT) if a bounded
+        wait of the last forward / adjoint in (mode, want_grad) gave up."""
+        d = self.dims()
+        ws = self.workspace(mode, want_grad)
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _cabi.call('mb_rime_status', self.mb_dtype, _cabi.MODES[mode], ctypes.byref(d), int(want_grad), ptr(ws),
+                   ws.numel(), ctypes.c_void_p(s.cuda_stream))
+
 
 class _RimeChi2(torch.autograd.Function):
     @staticmethod

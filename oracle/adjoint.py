@@ -190,13 +190,10 @@ def shape_grads(P, s0, s1, times=None):
     return c, d
 
 
-def chi2_grad(P, src_chunk=16):
-    """Return (chi^2, dict of gradients) in FP64."""
-    ntime, na = P['uvw'].shape[:2]
-    nbl = P['antenna1'].shape[1]
-    nchan = P['frequency'].shape[0]
-    nsrc = P['lm'].shape[0]
-    npsrc, ngsrc, nssrc = P['npsrc'], P['ngsrc'], P['nssrc']
+def chi2_grad_prepare(P, src_chunk=16):
+    """The per-visibility part of the gradient: chi^2, gV = d chi^2 / dV and
+    d chi^2 / dG (a dict the per-source part reads)."""
+    ntime = P['uvw'].shape[0]
     a1, a2 = P['antenna1'], P['antenna2']
     tt = np.arange(ntime)[:, None]
     V = O.ekb_vis(P, src_chunk=src_chunk)
@@ -219,52 +216,79 @@ def chi2_grad(P, src_chunk=16):
     for t in range(ntime):
         np.add.at(gG[t], a1[t], dGp[t])
         np.add.at(gG[t], a2[t], dGq[t])
+    return {'P': P, 'chi2': chi2, 'gV': gV, 'gG': gG}
 
+
+def chi2_grad_sources(base, s0, s1):
+    """Gradients of the source parameters of sources [s0, s1), from
+    chi2_grad_prepare's gV: (g_lm, g_stokes, g_alpha, g_shape) for those
+    sources, g_shape (3, s1 - s0) (zero for point sources)."""
+    P, gV = base['P'], base['gV']
+    ntime = P['uvw'].shape[0]
+    a1, a2 = P['antenna1'], P['antenna2']
+    tt = np.arange(ntime)[:, None]
+    f = P['frequency']
+    uvw = P['uvw']
+    sl = slice(s0, s1)
+    K = O.phase_scalar(P, sl)
+    Bs = O.brightness_sqrt(O.brightness(P, sl))
+    E, dE_dl, dE_dm = beam_with_grad(P, sl)
+    KB = K[..., None] * Bs[:, :, None]
+    J = O.jones_mul(E, KB)
+    Jp, Jq = J[:, tt, a1], J[:, tt, a2]
+    c, dc = shape_grads(P, s0, s1)
+    gJ = np.zeros_like(J)
+    cp = O.jones_mul(gV[None], Jq) * c[..., None]
+    cq = O.jones_mul(_herm(gV)[None], Jp) * c[..., None]
+    for t in range(ntime):
+        np.add.at(gJ[:, t], (slice(None), a1[t]), cp[:, t])
+        np.add.at(gJ[:, t], (slice(None), a2[t]), cq[:, t])
+    gc = _re_inner(gV[None], O.jones_mul_h(Jp, Jq))
+    g_shape = np.einsum('stbc,sktbc->ks', gc, dc)
+    gE = O.jones_mul_h(gJ, KB)
+    gKB = O.jones_mul(_herm(E), gJ)
+    gK = np.sum(np.conj(Bs)[:, :, None] * gKB, axis=-1)
+    gBs = (np.conj(K)[..., None] * gKB).sum(axis=2)
+    l, m = P['lm'][sl, 0], P['lm'][sl, 1]
+    nf = np.sqrt(1 - l ** 2 - m ** 2)
+    dphase = -2j * np.pi * f / O.LIGHTSPEED
+    dK = K * dphase[None, None, None, :]
+    dphi_dl = uvw[None, :, :, 0] - uvw[None, :, :, 2] * (l / nf)[:, None, None]
+    dphi_dm = uvw[None, :, :, 1] - uvw[None, :, :, 2] * (m / nf)[:, None, None]
+    gphi = (np.conj(gK) * dK).real
+    g_lm = np.stack([(gphi * dphi_dl[..., None]).sum(axis=(1, 2, 3)) + _re_inner(gE, dE_dl).sum(axis=(1, 2, 3)),
+                     (gphi * dphi_dm[..., None]).sum(axis=(1, 2, 3)) + _re_inner(gE, dE_dm).sum(axis=(1, 2, 3))],
+                    axis=-1)
+    g_stokes, g_alpha = brightness_sqrt_grads(P, gBs, sl)
+    return s0, s1, g_lm, g_stokes, g_alpha, g_shape
+
+
+def chi2_grad_combine(base, parts):
+    """(chi^2, dict of gradients) from chi2_grad_prepare and the
+    chi2_grad_sources results of batches covering every source once."""
+    P = base['P']
+    npsrc, ngsrc = P['npsrc'], P['ngsrc']
     g_lm = np.zeros_like(P['lm'])
     g_stokes = np.zeros_like(P['stokes'])
     g_alpha = np.zeros_like(P['alpha'])
     g_gauss = np.zeros_like(P['gauss_shape'])
     g_sersic = np.zeros_like(P['sersic_shape'])
-    f = P['frequency']
-    uvw = P['uvw']
-    for s0 in range(0, nsrc, src_chunk):
-        s1 = min(nsrc, s0 + src_chunk)
-        sl = slice(s0, s1)
-        K = O.phase_scalar(P, sl)
-        Bs = O.brightness_sqrt(O.brightness(P, sl))
-        E, dE_dl, dE_dm = beam_with_grad(P, sl)
-        KB = K[..., None] * Bs[:, :, None]
-        J = O.jones_mul(E, KB)
-        Jp, Jq = J[:, tt, a1], J[:, tt, a2]
-        c, dc = shape_grads(P, s0, s1)
-        gJ = np.zeros_like(J)
-        cp = O.jones_mul(gV[None], Jq) * c[..., None]
-        cq = O.jones_mul(_herm(gV)[None], Jp) * c[..., None]
-        for t in range(ntime):
-            np.add.at(gJ[:, t], (slice(None), a1[t]), cp[:, t])
-            np.add.at(gJ[:, t], (slice(None), a2[t]), cq[:, t])
-        gc = _re_inner(gV[None], O.jones_mul_h(Jp, Jq))
-        gsh = np.einsum('stbc,sktbc->sk', gc, dc)
+    for s0, s1, gl, gs, ga, gsh in parts:
+        g_lm[s0:s1] += gl
+        g_stokes[s0:s1] += gs
+        g_alpha[s0:s1] += ga
         for s in range(s0, s1):
             if npsrc <= s < npsrc + ngsrc:
-                g_gauss[:, s - npsrc] += gsh[s - s0]
+                g_gauss[:, s - npsrc] += gsh[:, s - s0]
             elif s >= npsrc + ngsrc:
-                g_sersic[:, s - npsrc - ngsrc] += gsh[s - s0]
-        gE = O.jones_mul_h(gJ, KB)
-        gKB = O.jones_mul(_herm(E), gJ)
-        gK = np.sum(np.conj(Bs)[:, :, None] * gKB, axis=-1)
-        gBs = (np.conj(K)[..., None] * gKB).sum(axis=2)
-        l, m = P['lm'][sl, 0], P['lm'][sl, 1]
-        nf = np.sqrt(1 - l ** 2 - m ** 2)
-        dphase = -2j * np.pi * f / O.LIGHTSPEED
-        dK = K * dphase[None, None, None, :]
-        dphi_dl = uvw[None, :, :, 0] - uvw[None, :, :, 2] * (l / nf)[:, None, None]
-        dphi_dm = uvw[None, :, :, 1] - uvw[None, :, :, 2] * (m / nf)[:, None, None]
-        gphi = (np.conj(gK) * dK).real
-        g_lm[sl, 0] += (gphi * dphi_dl[..., None]).sum(axis=(1, 2, 3)) + _re_inner(gE, dE_dl).sum(axis=(1, 2, 3))
-        g_lm[sl, 1] += (gphi * dphi_dm[..., None]).sum(axis=(1, 2, 3)) + _re_inner(gE, dE_dm).sum(axis=(1, 2, 3))
-        gst, gal = brightness_sqrt_grads(P, gBs, sl)
-        g_stokes[sl] += gst
-        g_alpha[sl] += gal
-    return chi2, {'lm': g_lm, 'stokes': g_stokes, 'alpha': g_alpha, 'gauss_shape': g_gauss,
-                  'sersic_shape': g_sersic, 'G_term': gG}
+                g_sersic[:, s - npsrc - ngsrc] += gsh[:, s - s0]
+    return base['chi2'], {'lm': g_lm, 'stokes': g_stokes, 'alpha': g_alpha, 'gauss_shape': g_gauss,
+                          'sersic_shape': g_sersic, 'G_term': base['gG']}
+
+
+def chi2_grad(P, src_chunk=16):
+    """Return (chi^2, dict of gradients) in FP64."""
+    base = chi2_grad_prepare(P, src_chunk)
+    nsrc = P['lm'].shape[0]
+    parts = [chi2_grad_sources(base, s0, min(nsrc, s0 + src_chunk)) for s0 in range(0, nsrc, src_chunk)]
+    return chi2_grad_combine(base, parts)

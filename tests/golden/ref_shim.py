@@ -19,12 +19,25 @@ arithmetic:
 """
 import importlib.util
 import logging
+import os
 import sys
 import types
 
 import numpy as np
 
-REF_ROOT = '/root/reference/montblanc'
+#: The reference checkout's ``montblanc`` package directory: the
+#: MONTBLANC_REFERENCE environment variable names the checkout (default
+#: /root/reference); ``set_reference_root`` overrides it before first use.
+REF_ROOT = os.path.join(os.environ.get('MONTBLANC_REFERENCE', '/root/reference'), 'montblanc')
+
+
+def set_reference_root(checkout):
+    """Load the reference from the checkout at ``checkout`` (call before
+    the first ``reference_solver``)."""
+    global REF_ROOT
+    if _CPUSolver is not None:
+        raise RuntimeError('the reference CPUSolver is already loaded from %s' % REF_ROOT)
+    REF_ROOT = os.path.join(checkout, 'montblanc')
 
 
 def _numexpr_module():

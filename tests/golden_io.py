@@ -39,3 +39,19 @@ def rel_err(a, b):
     b = np.asarray(b)
     den = np.max(np.abs(b))
     return float(np.max(np.abs(a - b)) / (den if den > 0 else 1.0))
+
+
+def conditioning(P, ref):
+    """kappa = max |model| / max |observed - model|: a chi^2 term is the
+    square of a residual that is small against the model, so a relative
+    error e of the model visibilities becomes a relative error of about
+    2 e kappa in the chi^2 terms."""
+    vis = np.asarray(ref['vis_out'])
+    res = np.asarray(P['observed_vis']) - vis
+    return float(np.max(np.abs(vis)) / max(np.max(np.abs(res)), 1e-300))
+
+
+def terms_tol(P, ref, vis_rel, floor):
+    """Bound on rel_err of the chi^2 terms implied by model visibilities
+    that agree to ``vis_rel`` (relative), never below ``floor``."""
+    return max(floor, 2.0 * vis_rel * conditioning(P, ref))

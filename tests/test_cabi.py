@@ -12,7 +12,7 @@ HEADER = os.path.join(ROOT, 'include', 'montblanc_gb300.h')
 
 def declared_functions():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r'^\s*(?:const char\*|mb_status|size_t|uint64_t)\s+(mb_\w+)\s*\(', text, re.M)))
+    return sorted(set(re.findall(r'^\s*(?:const char\*|mb_status|size_t|uint64_t|uint32_t)\s+(mb_\w+)\s*\(', text, re.M)))
 
 
 def test_header_declares_entry_points():

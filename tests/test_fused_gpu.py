@@ -19,7 +19,10 @@ def test_fused_solver_matches_reference(name, dtype):
     with solver_for(P, dtype, mb.Pipeline([mb.RimeV4Fused()])) as s:
         s.solve()
         assert golden_io.rel_err(s.retrieve_model_vis(), ref['vis_out']) < TOL[dtype]['vis']
-        assert golden_io.rel_err(s.retrieve_chi_sqrd_result(), ref['chi_sqrd_terms']) < TOL[dtype]['terms']
+        # chi^2 terms: the model's agreement amplified by max|model| / max|residual|
+        vis_rel = 1e-12 if dtype == 'double' else 2e-7
+        assert golden_io.rel_err(s.retrieve_chi_sqrd_result(), ref['chi_sqrd_terms']) < \
+            golden_io.terms_tol(P, ref, vis_rel, TOL[dtype]['terms'])
         assert abs(s.X2 - ref['X2']) <= TOL[dtype]['X2'] * abs(ref['X2'])
 
 

@@ -19,9 +19,12 @@ def test_oracle_matches_reference(name):
     jones = P.get('jones')
     out, terms, X2 = O.forward(P, src_chunk=8, jones=jones)
     # chi^2 terms are squared residuals of nearly equal quantities, so their
-    # relative error is larger than that of the model; 1e-10 is the FP64 bar.
+    # relative error is that of the model amplified by max|model| /
+    # max|residual| (7000 on the 20 500-source units: sums over sources in
+    # a different order than the reference's differ by ~1e-14); 1e-10 is
+    # the FP64 bar where that amplification is small.
     assert golden_io.rel_err(out, ref['vis_out']) < 1e-11
-    assert golden_io.rel_err(terms, ref['chi_sqrd_terms']) < 1e-10
+    assert golden_io.rel_err(terms, ref['chi_sqrd_terms']) < golden_io.terms_tol(P, ref, 1e-13, 1e-10)
     assert abs(X2 - ref['X2']) <= 1e-10 * abs(ref['X2'])
     if 'B_sqrt' in ref:
         assert golden_io.rel_err(O.brightness_sqrt(O.brightness(P)), ref['B_sqrt']) < 1e-13

@@ -135,3 +135,50 @@ def test_bounded_wait_gives_up_and_the_context_stays_usable(limit):
     assert status.item() == 0
     ref = (A.double() @ B.double().T)
     assert float((D.double() - ref).abs().max() / ref.abs().max()) < 5e-6
+
+
+def test_fused_timeout_reaches_the_host():
+    """With the poll limit of the tensor-core kernels' pipeline waits at 0,
+    every such wait gives up at once: the forward's chi^2 is NaN and
+    mb_rime_status reports MB_ERR_TIMEOUT, and so does an adjoint after it
+    (which then does no work).  An adjoint after a good forward gives up on
+    its own waits and reports it too.  With the default limit restored the
+    same problem runs correctly in the same context."""
+    import math
+    import torch
+    import golden_io
+    from montblanc_gb300 import _cabi
+    from montblanc_gb300.rime import RimeProblem
+    P, ref = golden_io.load('small_fp64')
+    prob = RimeProblem.from_numpy(P, dtype='float')
+    good = prob.forward(mode='split_tf32', want_grad=True).item()
+    prob.adjoint(mode='split_tf32')
+    prob.check('split_tf32', True)
+    default = _cabi.lib.mb_default_wait_limit()
+    try:
+        _cabi.call('mb_set_wait_limit', 0)
+        x2 = prob.forward(mode='split_tf32', want_grad=True).item()
+        assert math.isnan(x2)
+        with pytest.raises(_cabi.MontblancError) as e:
+            prob.check('split_tf32', True)
+        assert e.value.status == 6  # MB_ERR_TIMEOUT
+        prob.adjoint(mode='split_tf32')
+        with pytest.raises(_cabi.MontblancError):
+            prob.check('split_tf32', True)
+        # a good forward, then an adjoint whose own waits give up
+        _cabi.call('mb_set_wait_limit', default)
+        prob.forward(mode='split_tf32', want_grad=True)
+        torch.cuda.synchronize()
+        _cabi.call('mb_set_wait_limit', 0)
+        prob.adjoint(mode='split_tf32')
+        with pytest.raises(_cabi.MontblancError):
+            prob.check('split_tf32', True)
+    finally:
+        torch.cuda.synchronize()
+        _cabi.call('mb_set_wait_limit', default)
+    x2 = prob.forward(mode='split_tf32', want_grad=True).item()
+    g = prob.adjoint(mode='split_tf32')
+    prob.check('split_tf32', True)
+    assert x2 == good
+    assert abs(x2 - ref['X2']) <= 1e-4 * abs(ref['X2'])
+    assert all(torch.isfinite(v).all() for v in g.values())
