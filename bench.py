@@ -35,25 +35,52 @@ sys.path.insert(0, ROOT)
 METRIC = 'source·vis terms/s for χ²+grad, split-prec vs plain FP32, at stated FP64 error'
 UNIT = 'source·vis terms/s'
 
-# Algorithmic work per source.vis term: a 2x2 complex J_p J_q^H product with
-# accumulation (64 flops) forward; the two 2x2 complex products of the
-# adjoint, d/dJ_p += gV J_q and d/dJ_q += gV^H J_p (128 flops).
+# Algorithmic work per source.vis term: one 2x2 complex J_p J_q^H product with
+# its accumulation, 64 flops, in the forward; the adjoint's X.A contraction
+# (d chi^2 / dJ_a = sum_b Y_ab J_b), 64 flops.  chi^2 + gradient: 128.
 FLOPS_FWD = 64
-FLOPS_ADJ = 128
+FLOPS_ADJ = 64
 SM_COUNT = 152
 
-# DRAM traffic (bytes) per launch of the dominant kernel from ncu captures,
-# keyed by (kernel, workload, mode).
-NCU_TRAFFIC = {
-    # ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum (one pass), the
-    # timed step of `bench.py --steps 1 --warmup 1 --no-e2e --no-cpu
-    # --no-plain --no-batch`
-    ('coh_tc_adj_kernel', 'large_point', 'split_tf32'): 9.34e9 + 0.199e9,
-    ('coh_tc_fwd_kernel', 'large_point', 'split_tf32'): 6.29e9 + 3.42e9,
-    # the same with --workload profile_point
-    ('coh_tc_adj_kernel', 'profile_point', 'split_tf32'): 351.6e6 + 4.1e6,
-    ('coh_tc_fwd_kernel', 'profile_point', 'split_tf32'): 229.3e6 + 108.9e6,
+# What ncu shows for the dominant kernels (profiles/*.md of the same build:
+# one --set full capture of one launch on the profile_point workload).
+NCU_LIMITER = {
+    'coh_tc_adj_kernel': {
+        'source': 'profiles/coh_tc_adj_kernel_profile_point.md',
+        'limiter': 'CUDA-core issue and latency of the per-(source, antenna) producer and chain',
+        'sm__pipe_tensor_cycles_active': 0.097, 'smsp__issue_active': 0.448,
+        'pipe_fma': 0.261, 'pipe_alu': 0.245, 'pipe_fp64': 0.055, 'pipe_xu': 0.042},
+    'coh_tc_fwd_kernel': {
+        'source': 'profiles/coh_tc_fwd_kernel_profile_point.md',
+        'limiter': 'CUDA-core issue and latency of the per-(source, antenna) producer; TMEM drains',
+        'sm__pipe_tensor_cycles_active': 0.281, 'smsp__issue_active': 0.438,
+        'pipe_fma': 0.192, 'pipe_alu': 0.329, 'pipe_fp64': 0.070, 'pipe_xu': 0.038},
 }
+
+# DRAM bytes per launch from a one-kernel ncu capture on the profile_point
+# workload (32 x 64 x 64 units, 4000 point + 50 gaussian sources; profiles/
+# dram_bytes_profile_point.md), split into the part that scales with the
+# (time, channel) units and the part that scales with the (time, source,
+# antenna) path lengths, read once per time step from DRAM (the units of one
+# time step run together and share them in L2).
+NCU_DRAM = {
+    # kernel: (bytes per unit, bytes per (time, source, antenna))
+    'coh_tc_adj_kernel': (131072.0 + 2000.0, 8.0),
+    'coh_tc_fwd_kernel': (165000.0, 8.0),
+}
+
+
+def dram_traffic(kernel, workload):
+    """Modelled DRAM bytes per launch of ``kernel`` on ``workload`` (None if
+    the kernel has no capture)."""
+    from montblanc_gb300 import synth
+    if kernel not in NCU_DRAM:
+        return None
+    w = synth.WORKLOADS[workload]
+    per_unit, per_tsa = NCU_DRAM[kernel]
+    units = w['ntime'] * w['nchan']
+    tsa = w['ntime'] * (w['npsrc'] + w['ngsrc'] + w['nssrc']) * w['na']
+    return per_unit * units + per_tsa * tsa
 
 
 def workload_terms(name):
@@ -64,38 +91,60 @@ def workload_terms(name):
     return w['npsrc'] * vis, (w['ngsrc'] + w['nssrc']) * vis
 
 
-def roofline(workload, mode, kernels, peak, peak_src, clk):
-    """Roofline of the kernel with the largest share of the timed steps.
-
-    achieved = algorithmic flops per launch / mean CUDA-event duration of
-    that kernel's launches in the timed region (events on its launch
-    stream).  Algorithmic flops: FLOPS_FWD per source.vis term for the
-    forward coherency kernels, FLOPS_ADJ per term for the adjoint kernels,
-    over the sources each kernel handles (split modes: the tensor-core
-    kernels take the point sources; the CUDA-core adjoint the rest)."""
+def kernel_work(workload, mode):
+    """Algorithmic flops per launch of each coherency kernel: FLOPS_FWD per
+    source.vis term for the forward kernels, FLOPS_ADJ per term for the
+    adjoint kernels, over the sources each kernel handles (split modes: the
+    tensor-core kernels take the point sources, the forward kernel also the
+    extended ones; the CUDA-core adjoint the extended sources)."""
     pt, et = workload_terms(workload)
     split = mode != 'native'
-    work = {
+    return {
         'coh_tc_fwd_kernel': FLOPS_FWD * (pt + et),
         'coh_fwd_kernel': FLOPS_FWD * (pt + et),
         'coh_tc_adj_kernel': FLOPS_ADJ * pt,
         'coh_adj_kernel': FLOPS_ADJ * (et if split else pt + et),
     }
+
+
+def fp32_peak_tflops(clk):
+    """FP32 CUDA-core peak at the sampled SM clock (152 SMs x 128 FMA)."""
+    sm_mhz = clk.get('sm_mhz') or 2070.0
+    return SM_COUNT * 128 * 2 * sm_mhz * 1e6 / 1e12
+
+
+def roofline(workload, mode, kernels, peak, peak_src, clk):
+    """Roofline of the kernel with the largest share of the timed steps.
+
+    achieved = algorithmic flops per launch / mean CUDA-event duration of
+    that kernel's launches in the timed region (events on its launch
+    stream), against the measured sustained bf16 tensor peak for the
+    tensor-core forms (the roof of the contraction they execute) and the
+    FP32 CUDA-core peak at the sampled clock for the plain form.  The bound
+    is the roof the kernel's arithmetic intensity puts it under; ``limiter``
+    is what ncu shows holding it below that roof."""
+    work = kernel_work(workload, mode)
     name = max(kernels, key=lambda k: kernels[k][0])
     ms, n = kernels[name]
     per_launch_ms = ms / n
     flops = work.get(name)
-    sm_mhz = clk.get('sm_mhz') or 2070.0
-    fp32_peak = SM_COUNT * 128 * 2 * sm_mhz * 1e6 / 1e12
-    out = {'bound': 'tensor', 'kernel': name, 'launch_ms': per_launch_ms, 'unit': 'TFLOP/s',
-           'peak': peak, 'peak_source': '%s bf16 sustained (MEASURED_PEAKS.json)' % peak_src,
-           'traffic': NCU_TRAFFIC.get((name, workload, mode))}
+    if mode == 'native':
+        out = {'bound': 'fp32 (CUDA cores)', 'peak': fp32_peak_tflops(clk),
+               'peak_source': 'FP32 CUDA-core peak at the sampled SM clock'}
+    else:
+        out = {'bound': 'tensor', 'peak': peak,
+               'peak_source': '%s bf16 sustained (MEASURED_PEAKS.json)' % peak_src}
+    out.update({'kernel': name, 'launch_ms': per_launch_ms, 'unit': 'TFLOP/s',
+                'traffic': dram_traffic(name, workload),
+                'traffic_source': 'profiles/dram_bytes_profile_point.md, scaled by units and path lengths'})
+    if name in NCU_LIMITER:
+        out['limiter'] = NCU_LIMITER[name]
     if flops is None:
         out.update({'achieved': None, 'frac': None})
         return out
     achieved = flops / (per_launch_ms * 1e-3) / 1e12
-    out.update({'achieved': achieved, 'frac': achieved / peak, 'algorithmic_flops_per_launch': flops,
-                'fp32_simt_peak_tflops_at_clock': fp32_peak, 'fp32_simt_frac': achieved / fp32_peak})
+    out.update({'achieved': achieved, 'frac': achieved / out['peak'], 'algorithmic_flops_per_launch': flops,
+                'flops_per_term': FLOPS_ADJ if 'adj' in name else FLOPS_FWD})
     return out
 
 
@@ -338,36 +387,55 @@ def subset_problem(P, prob, times, chans):
     return Q
 
 
-def errors_vs_fp64(P, prob, mode):
-    """Visibility, chi^2 and gradient errors of ``mode`` against the FP64
-    GPU path (itself within 1e-10 of the reference CPU path) on 2 time steps
-    x 3 channels of the workload with every source and antenna."""
+ERROR_FIXTURES = (
+    ('units_medium_mixed', '3 time steps x 3 channels of the 100 x 27 x 64 workload, all 1250 sources '
+                           '(1000 point + 200 gaussian + 50 sersic) and 351 baselines'),
+    ('units_large_point', '2 time steps x 3 channels of the 200 x 64 x 256 workload (this benchmark\'s '
+                          'generator and seed), all 20500 sources and 2016 baselines'),
+)
+GRAD_NAMES = ('lm', 'stokes', 'alpha', 'gauss_shape', 'sersic_shape', 'G_term')
+
+
+def errors_vs_reference(modes):
+    """Errors of each form against the reference on sampled units of the two
+    large workloads (tests/golden fixtures: the reference's CPUSolver
+    outputs, run per source batch, and the FP64 oracle's gradients at the
+    truth and at displaced source positions; the reference has no
+    gradient).  Norm-wise relative errors; chi^2 relative."""
     import numpy as np
-    import torch
+    sys.path.insert(0, os.path.join(ROOT, 'tests'))
+    import golden_io
     from montblanc_gb300.rime import RimeProblem
-    Q = subset_problem(P, prob, [0, prob.ntime - 1], [0, prob.nchan // 2, prob.nchan - 1])
-    # the FP64 reference sees the same FP32 data, so the error is the method's
-    for k, v in list(Q.items()):
-        if isinstance(v, np.ndarray) and v.dtype == np.float64:
-            Q[k] = v.astype(np.float32).astype(np.float64)
-        elif isinstance(v, np.ndarray) and v.dtype == np.complex128:
-            Q[k] = v.astype(np.complex64).astype(np.complex128)
-    p64 = RimeProblem.from_numpy(Q, dtype='double')
-    p32 = RimeProblem.from_numpy(Q, dtype='float')
-    v64, v32 = p64.empty_vis(), p32.empty_vis()
-    x64, g64 = p64.forward(model_vis=v64, want_grad=True).item(), None
-    g64 = p64.adjoint()
-    x32 = p32.forward(mode=mode, model_vis=v32, want_grad=True).item()
-    g32 = p32.adjoint(mode=mode)
-    a, b = v32.cpu().numpy().astype(np.complex128), v64.cpu().numpy()
-    # the outputs are residual-free model visibilities (vis_output='model')
-    out = {'vis_rel_norm': float(np.linalg.norm(a - b) / np.linalg.norm(b)),
-           'vis_rel_max': float(np.max(np.abs(a - b)) / np.max(np.abs(b))),
-           'chi2_rel': abs(x32 - x64) / abs(x64)}
-    for k in ('lm', 'stokes', 'G_term'):
-        ga, gb = g32[k].cpu().numpy().astype(np.complex128), g64[k].cpu().numpy()
-        out['grad_%s_rel_norm' % k] = float(np.linalg.norm(ga - gb) / np.linalg.norm(gb))
-    out['sample'] = '2 time steps x 3 channels, all %d sources and %d antennas' % (prob.nsrc, prob.na)
+
+    def nerr(a, b):
+        return float(np.linalg.norm(np.asarray(a) - b) / np.linalg.norm(b))
+
+    out = {}
+    for name, desc in ERROR_FIXTURES:
+        P, ref = golden_io.load(name)
+        res = {'sample': desc, 'reference': 'reference CPUSolver forward; FP64 oracle gradient'}
+        for dtype, mode in [('double', 'native'), ('float', 'native')] + [('float', m) for m in modes]:
+            key = 'fp64' if dtype == 'double' else ('plain_fp32' if mode == 'native' else mode)
+            r = {}
+            for disp in (False, True):
+                Q = dict(P)
+                if disp:
+                    Q['lm'] = ref['displaced_lm']
+                prob = RimeProblem.from_numpy(Q, dtype=dtype)
+                vis = prob.empty_vis()
+                x2 = prob.forward(mode=mode, model_vis=vis, want_grad=True).item()
+                g = prob.adjoint(mode=mode)
+                prob.check(mode, True)
+                pre = 'displaced_grad_' if disp else 'grad_'
+                ge = {k: nerr(g[k].cpu().numpy(), ref[pre + k]) for k in GRAD_NAMES if ref[pre + k].size}
+                if disp:
+                    r['grad_displaced_rel_norm'] = ge
+                else:
+                    r['vis_rel_norm'] = nerr(vis.cpu().numpy(), ref['vis_out'])
+                    r['chi2_rel'] = abs(x2 - float(ref['X2'])) / abs(float(ref['X2']))
+                    r['grad_truth_rel_norm'] = ge
+            res[key] = r
+        out[name] = res
     return out
 
 
@@ -416,19 +484,39 @@ def time_resident(prob, mode, steps, warmup, ws, kernels=None):
     return total / steps, statistics.mean(fwd), statistics.mean(adj)
 
 
-def time_plain_slice(P, prob, ws, ntime=20):
-    import numpy as np
+def time_plain_slice(P, prob, ws, workload, clk, ntime=20, steps=3, warmup=1):
+    """The plain FP32 CUDA-core form on the first ``ntime`` time steps of
+    the workload (its throughput per term does not depend on the time
+    extent), ``steps`` timed steps after ``warmup``, with its own roofline
+    against the FP32 CUDA-core peak."""
     import torch
     from montblanc_gb300.rime import RimeProblem
     nt = min(ntime, prob.ntime)
     Q = subset_problem(P, prob, list(range(nt)), list(range(prob.nchan)))
     sub = RimeProblem.from_numpy(Q, dtype='float')
     terms = prob.nsrc * nt * prob.nbl * prob.nchan
-    ms, fwd, adj = time_resident(sub, 'native', 1, 1, ws)
+    kernels = {}
+    ms, fwd, adj = time_resident(sub, 'native', steps, warmup, ws, kernels)
+    sub.check('native', True)
     ms = max_over_ranks(ws, ms)
+    kernels.pop('_launches', None)
+    pt, et = workload_terms(workload)
+    scale = nt / prob.ntime  # the slice's share of the workload's terms
+    work = {'coh_fwd_kernel': FLOPS_FWD * (pt + et) * scale, 'coh_adj_kernel': FLOPS_ADJ * (pt + et) * scale}
+    peak = fp32_peak_tflops(clk)
+    rl = {}
+    for k, (kms, n) in kernels.items():
+        if k in work:
+            ach = work[k] / (kms / n * 1e-3) / 1e12
+            rl[k] = {'achieved': ach, 'unit': 'TFLOP/s', 'peak': peak, 'frac': ach / peak,
+                     'bound': 'fp32 (CUDA cores)', 'launch_ms': kms / n}
+    step_ach = (FLOPS_FWD + FLOPS_ADJ) * terms / (ms * 1e-3) / 1e12
     out = {'value': ws * terms / (ms * 1e-3), 'unit': UNIT, 'ms_per_step': ms, 'forward_ms': fwd,
-           'adjoint_ms': adj, 'mode': 'native',
-           'sample': 'first %d of %d time steps, all sources, baselines and channels' % (nt, prob.ntime)}
+           'adjoint_ms': adj, 'mode': 'native', 'steps': steps, 'warmup': warmup,
+           'sample': 'first %d of %d time steps, all sources, baselines and channels' % (nt, prob.ntime),
+           'roofline': {'step_achieved_tflops': step_ach, 'fp32_peak_tflops_at_clock': peak,
+                        'step_frac': step_ach / peak, 'kernels': rl},
+           'kernels_ms_per_step': {k: v[0] / steps for k, v in sorted(kernels.items())}}
     del sub
     torch.cuda.empty_cache()
     return out
@@ -477,7 +565,8 @@ def time_e2e(prob, mode, steps, warmup, ws):
 
 def cpu_baseline(P, prob, max_units=None):
     """The FP64 oracle (forward + gradient) on the host cores over a bounded
-    sample: (time, channel) units with all antennas and 2000 sources."""
+    sample: (time, channel) units with all antennas and 2000 sources drawn
+    from every source type in the workload's proportions."""
     from oracle import cpu_baseline as C
     cores = os.cpu_count() or 1
     nunits = max_units or 2 * cores
@@ -487,9 +576,12 @@ def cpu_baseline(P, prob, max_units=None):
     probs = C.make_units(P, lambda t, ch: obs[t, :, ch].cpu().numpy(), units, nsample)
     wall, procs = C.time_units(probs, cores)
     terms = nunits * nsample * prob.nbl
+    mix = C.sample_mix(P, nsample)
     return {'value': terms / wall, 'unit': UNIT, 'cores': procs, 'kind': 'port',
-            'sample': '%d (time, channel) units x %d sources x %d baselines, FP64 NumPy chi^2 + gradient, '
-                      '%.1f s wall' % (nunits, nsample, prob.nbl, wall)}
+            'sample': '%d (time, channel) units x %d sources (%d point + %d gaussian + %d sersic) x %d baselines, '
+                      'FP64 NumPy chi^2 + gradient (the oracle, a NumPy restatement of the reference\'s '
+                      'CPUSolver: the reference tree is not on the GPU machines), %.1f s wall'
+                      % (nunits, nsample, mix[0], mix[1], mix[2], prob.nbl, wall)}
 
 
 def peaks():
@@ -529,16 +621,31 @@ def run_reference(args):
             times.append(wall)
     terms = cores * nsample * nbl
     value = terms / statistics.mean(times)
+    mix = C.sample_mix(P, nsample)
     line = {'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': args.gpus,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * statistics.mean(times),
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
             'data': 'synthetic',
-            'config': {'workload': workload_desc(args.workload), 'form': 'CPU FP64 (reference algorithm)'},
+            'config': run_config(args, 1),
+            'form': 'CPU FP64 chi^2 + gradient: the oracle, a NumPy restatement of the reference\'s v4 CPUSolver '
+                    '(the reference tree is not on the GPU machines; the restatement is faster than the '
+                    'reference\'s own code, so the ratio against it is conservative)',
             'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': procs, 'kind': 'port',
-                             'sample': 'per step %d (time, channel) units x %d sources x %d baselines'
-                                       % (cores, nsample, nbl)},
+                             'sample': 'per step %d (time, channel) units x %d sources (%d point + %d gaussian '
+                                       '+ %d sersic, in the workload\'s proportions) x %d baselines'
+                                       % (cores, nsample, mix[0], mix[1], mix[2], nbl)},
             'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line))
+
+
+def run_config(args, ws):
+    """The workload configuration both arms report."""
+    from montblanc_gb300 import synth
+    w = synth.WORKLOADS[args.workload]
+    nvis = w['ntime'] * synth.nr_of_baselines(w['na']) * w['nchan']
+    return {'workload': workload_desc(args.workload), 'mode': args.mode, 'terms_per_step': terms_of(args.workload),
+            'l2': 'inputs larger than L2 (observed_vis alone %.1f GB)' % (nvis * 4 * 8 / 1e9),
+            'phase': 'FP64 argument and range reduction', 'replicas': ws}
 
 
 def main():
@@ -555,6 +662,7 @@ def main():
     kernels = {}
     ms, fwd_ms, adj_ms = time_resident(prob, args.mode, args.steps, args.warmup, ws, kernels)
     clk = clocks.stop()
+    prob.check(args.mode, True)  # no bounded device wait gave up
     ms_max = max_over_ranks(ws, ms)
     value = whole_job_value(ws, terms, ms_max)
 
@@ -562,7 +670,7 @@ def main():
     if not args.no_plain and args.mode != 'native':
         # The plain FP32 CUDA-core form on the first 20 time steps of the same
         # workload (throughput per term does not depend on the time extent).
-        plain = time_plain_slice(P, prob, ws)
+        plain = time_plain_slice(P, prob, ws, args.workload, clk)
     e2e = None
     if not args.no_e2e:
         ems, h2d, d2h, phases = time_e2e(prob, args.mode, args.steps, 1, ws)
@@ -573,7 +681,7 @@ def main():
 
     if rank != 0:
         return
-    errs = errors_vs_fp64(P, prob, args.mode)
+    errs = errors_vs_reference(sorted({args.mode, 'split_tf32', 'split_bf16'} - {'native'}))
     burst, sustained, hbm, src = peaks()
     launches = kernels.pop('_launches')
     rl = roofline(args.workload, args.mode, kernels, sustained, src, clk)
@@ -582,20 +690,18 @@ def main():
         'warmup': args.warmup, 'ms_per_step': ms_max, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f32' if args.mode == 'native' else 'f32 (%s products)' % args.mode,
         'data': 'synthetic (seeded generator; observed = model + N(0,0.1) noise)',
-        'config': {'workload': workload_desc(args.workload), 'mode': args.mode, 'terms_per_step': terms,
-                   'l2': 'inputs larger than L2 (observed_vis alone %.1f GB)'
-                         % (prob.arrays['observed_vis'].numel() * 8 / 1e9),
-                   'phase': 'FP64 argument and range reduction', 'replicas': ws},
+        'config': run_config(args, ws),
         'forward_ms': fwd_ms, 'adjoint_ms': adj_ms,
         'roofline': rl,
         'kernels_ms_per_step': {k: v[0] / args.steps for k, v in sorted(kernels.items())},
-        'errors_vs_fp64': errs,
+        'errors_vs_reference': errs,
         'gpu_launches': launches,
         'clocks': clk,
     }
     if plain:
         line['plain_fp32'] = plain
         line['split_over_plain'] = value / plain['value']
+        line['roofline_plain_fp32'] = plain['roofline']
     if e2e:
         line['e2e'] = e2e
     if not args.no_cpu:

@@ -23,22 +23,35 @@ def _unit_worker(args):
     return chi2, time.perf_counter() - t0
 
 
+def sample_mix(P_full, nsrc_sample):
+    """(point, gaussian, sersic) counts of a sample of ``nsrc_sample``
+    sources in the problem's proportions (every type present keeps at least
+    one source)."""
+    counts = [P_full['npsrc'], P_full['ngsrc'], P_full['nssrc']]
+    total = sum(counts)
+    n = min(nsrc_sample, total)
+    mix = [min(c, max(1 if c else 0, int(round(n * c / total)))) for c in counts]
+    i = int(np.argmax(counts))
+    mix[i] = min(counts[i], mix[i] + n - sum(mix))
+    return tuple(mix)
+
+
 def make_units(P_full, obs, units, nsrc_sample):
-    """Sub-problems of one time step x one channel with the first
-    ``nsrc_sample`` sources (point sources first, as ordered).
+    """Sub-problems of one time step x one channel with ``nsrc_sample``
+    sources: the first sources of each type, in the problem's proportions
+    (sample_mix).
 
     ``obs(t, ch)`` returns the observed visibilities (nbl, 4) of a unit."""
     npsrc, ngsrc = P_full['npsrc'], P_full['ngsrc']
-    ns_p = min(npsrc, nsrc_sample)
-    ns_g = min(ngsrc, nsrc_sample - ns_p)
-    sel = np.r_[0:ns_p, npsrc:npsrc + ns_g]
+    ns_p, ns_g, ns_s = sample_mix(P_full, nsrc_sample)
+    sel = np.r_[0:ns_p, npsrc:npsrc + ns_g, npsrc + ngsrc:npsrc + ngsrc + ns_s]
     out = []
     for (t, ch) in units:
         P = {k: P_full[k] for k in ('gauss_scale', 'two_pi_over_c', 'sigma_sqrd', 'beam_ll', 'beam_lm',
                                     'beam_lfreq', 'beam_ul', 'beam_um', 'beam_ufreq', 'E_beam',
                                     'antenna_scaling')}
         P['antenna_scaling'] = P_full['antenna_scaling'][:, ch:ch + 1]
-        P.update(npsrc=ns_p, ngsrc=ns_g, nssrc=0, use_weight_vector=False, residuals=False)
+        P.update(npsrc=ns_p, ngsrc=ns_g, nssrc=ns_s, use_weight_vector=False, residuals=False)
         P['uvw'] = P_full['uvw'][t:t + 1]
         P['parallactic_angles'] = P_full['parallactic_angles'][t:t + 1]
         P['antenna1'] = P_full['antenna1'][t:t + 1]
@@ -51,7 +64,7 @@ def make_units(P_full, obs, units, nsrc_sample):
         P['stokes'] = P_full['stokes'][sel][:, t:t + 1]
         P['alpha'] = P_full['alpha'][sel][:, t:t + 1]
         P['gauss_shape'] = P_full['gauss_shape'][:, :ns_g]
-        P['sersic_shape'] = np.zeros((3, 0))
+        P['sersic_shape'] = P_full['sersic_shape'][:, :ns_s]
         nbl = P['antenna1'].shape[1]
         P['flag'] = np.zeros((1, nbl, 1, 4), np.uint8)
         P['weight_vector'] = np.ones((1, nbl, 1, 4))
