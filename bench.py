@@ -64,9 +64,11 @@ NCU_LIMITER = {
 # antenna) path lengths, read once per time step from DRAM (the units of one
 # time step run together and share them in L2).
 NCU_DRAM = {
-    # kernel: (bytes per unit, bytes per (time, source, antenna))
-    'coh_tc_adj_kernel': (131072.0 + 2000.0, 8.0),
-    'coh_tc_fwd_kernel': (165000.0, 8.0),
+    # kernel: (bytes per unit, bytes per (time, source, antenna)); the
+    # profile_point launch moved 334.5 MB (forward) and 353.0 MB (adjoint)
+    # over 2048 units and 32 x 4050 x 64 FP64 path lengths (66.4 MB)
+    'coh_tc_fwd_kernel': (145.1e3, 8.0),
+    'coh_tc_adj_kernel': (139.9e3, 8.0),
 }
 
 

@@ -178,6 +178,14 @@ __device__ __forceinline__ double mb_log(double x) { return log(x); }
 template <typename T> __device__ __forceinline__ T mb_clamp(T x, T lo, T hi) { return x < lo ? lo : (x > hi ? hi : x); }
 template <typename T> __device__ __forceinline__ T cabs_(Cx<T> z) { return mb_sqrt(z.r * z.r + z.i * z.i); }
 
+// X B for a Hermitian B = [[a, b], [conj(b), d]] with real a, d (a
+// brightness square root).
+template <typename T>
+__device__ __forceinline__ Jones<T> jmul_herm_real_diag(const Jones<T>& X, T a, T d, Cx<T> b) {
+  const Cx<T> bc = conj(b);
+  return {X.a * a + cmul(X.b, bc), cmul(X.a, b) + X.b * d, X.c * a + cmul(X.d, bc), cmul(X.c, b) + X.d * d};
+}
+
 // ---- brightness square root (a1) -----------------------------------------
 // B = [[I+Q, U+iV], [U-iV, I-Q]] * (nu/nu_ref)^alpha,
 // sqrt(B) = (B + s*1) / t with s = sqrt(det B), t = sqrt(tr B + 2 s); t := 1
@@ -358,46 +366,72 @@ __device__ __forceinline__ Jones<T> beam_interp(const T* __restrict__ E_beam, co
   return E;
 }
 
-// The beam cube blended along frequency for one channel: per (l, m) grid
-// cell the 4 correlations of E (complex) and of |E|, each linearly
-// interpolated between the two channel planes the channel falls between.
-// Trilinear interpolation of the cube is then a bilinear interpolation of
-// this plane with the same weights (sum over 8 corners = sum over 4 corners
-// of the channel-blended values).  Layout: [il][im][12] = E (4 complex),
-// |E| (4 real).
-constexpr int kPlaneVals = 12;
+// The beam cube blended along frequency for one channel, stored per (l, m)
+// grid cell as bilinear coefficients.  Per cell (i, j), the 12 values v
+// (the 4 correlations of E, complex, and of |E|), each linearly
+// interpolated between the two cube planes the channel falls between, give
+//   f00 = v(i, j),  a = v(i1, j) - v(i, j),  b = v(i, j1) - v(i, j),
+//   c = v(i1, j1) - v(i1, j) - b,   i1 = min(i + 1, lw - 1), j1 = min(j + 1, mh - 1),
+// stored as [f00 | a | b | c] (12 values each, 48 per cell), so that the
+// trilinear interpolation of the cube at (i + x, j + y, channel) is
+//   v = f00 + x a + y (b + x c),  dv/dx = a + y c,  dv/dy = b + x c:
+// the same weights as the 8-corner sum (the blend along frequency first),
+// three FMAs per value, and one contiguous cell per lookup.
+constexpr int kPlaneComp = 12;  // values per coefficient (E: 8, |E|: 4)
+constexpr int kPlaneVals = 4 * kPlaneComp;
+
+// The 12 bilinear values (and optionally their x and y derivatives) of the
+// coefficient cell at p for offsets x, y.
+template <typename T, bool DERIV>
+__device__ __forceinline__ void plane_cell(const T* __restrict__ p, T x, T y, T (&v)[kPlaneComp],
+                                           T (&dx)[kPlaneComp], T (&dy)[kPlaneComp]) {
+  if constexpr (sizeof(T) == 4) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {  // float4 runs: E.a E.b | E.c E.d | |E|
+      const float4 f4 = __ldg(q + r), a4 = __ldg(q + 3 + r), b4 = __ldg(q + 6 + r), c4 = __ldg(q + 9 + r);
+      const float f[4] = {f4.x, f4.y, f4.z, f4.w}, a[4] = {a4.x, a4.y, a4.z, a4.w};
+      const float b[4] = {b4.x, b4.y, b4.z, b4.w}, c[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float fy = fmaf(x, c[k], b[k]);
+        v[4 * r + k] = fmaf(y, fy, fmaf(x, a[k], f[k]));
+        if (DERIV) {
+          dx[4 * r + k] = fmaf(y, c[k], a[k]);
+          dy[4 * r + k] = fy;
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kPlaneComp; ++k) {
+      const T f = __ldg(p + k), a = __ldg(p + kPlaneComp + k), b = __ldg(p + 2 * kPlaneComp + k),
+              c = __ldg(p + 3 * kPlaneComp + k);
+      const T fy = b + x * c;
+      v[k] = f + x * a + y * fy;
+      if (DERIV) {
+        dx[k] = a + y * c;
+        dy[k] = fy;
+      }
+    }
+  }
+}
 
 template <typename T>
-__device__ __forceinline__ void plane_corner(const T* __restrict__ plane, int mh, int il, int im, T w,
-                                             Jones<T>& sum, T (&amp)[4]) {
-  const T* p = plane + kPlaneVals * (size_t(il) * mh + im);
-  Jones<T> e = jldg<T>(p);
-  sum.a = sum.a + e.a * w; sum.b = sum.b + e.b * w;
-  sum.c = sum.c + e.c * w; sum.d = sum.d + e.d * w;
-  if constexpr (sizeof(T) == 4) {  // 48-byte entries: |E| starts 16-byte aligned
-    const float4 ab = __ldg(reinterpret_cast<const float4*>(p + 8));
-    amp[0] += w * ab.x; amp[1] += w * ab.y; amp[2] += w * ab.z; amp[3] += w * ab.w;
-  } else {
-    amp[0] += w * __ldg(p + 8); amp[1] += w * __ldg(p + 9);
-    amp[2] += w * __ldg(p + 10); amp[3] += w * __ldg(p + 11);
-  }
+__device__ __forceinline__ const T* plane_cell_ptr(const T* plane, int mh, int il, int im) {
+  return plane + kPlaneVals * (size_t(il) * mh + im);
 }
 
 template <typename T>
 __device__ __forceinline__ Jones<T> beam_interp_plane(const T* __restrict__ plane, int mh, const GridPos<T>& gl,
                                                       const GridPos<T>& gm) {
-  Jones<T> sum = jzero<T>();
-  T amp[4] = {T(0), T(0), T(0), T(0)};
-  const T ld = gl.d, md = gm.d;
-  plane_corner(plane, mh, gl.i0, gm.i0, (T(1) - ld) * (T(1) - md), sum, amp);
-  plane_corner(plane, mh, gl.i1, gm.i0, ld * (T(1) - md), sum, amp);
-  plane_corner(plane, mh, gl.i0, gm.i1, (T(1) - ld) * md, sum, amp);
-  plane_corner(plane, mh, gl.i1, gm.i1, ld * md, sum, amp);
+  T v[kPlaneComp], unused[kPlaneComp];
+  plane_cell<T, false>(plane_cell_ptr(plane, mh, gl.i0, gm.i0), gl.d, gm.d, v, unused, unused);
   Jones<T> E;
-  E.a = renorm(sum.a, amp[0]);
-  E.b = renorm(sum.b, amp[1]);
-  E.c = renorm(sum.c, amp[2]);
-  E.d = renorm(sum.d, amp[3]);
+  E.a = renorm(Cx<T>{v[0], v[1]}, v[8]);
+  E.b = renorm(Cx<T>{v[2], v[3]}, v[9]);
+  E.c = renorm(Cx<T>{v[4], v[5]}, v[10]);
+  E.d = renorm(Cx<T>{v[6], v[7]}, v[11]);
   return E;
 }
 

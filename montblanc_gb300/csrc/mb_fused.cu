@@ -808,9 +808,21 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
     // the MMA warp's waits then give up too, and everyone reaches the end.
     for (int g = 0; g < nstages; ++g) {
       const int slot = g % kTcStages, use = g / kTcStages;
+      const int s0 = g * NSRC, ns = min(NSRC, A.npsrc - s0);
+      if (g + 1 < nstages && A.phi != nullptr) {  // the next stage's source terms into L1
+        const int sn = s0 + NSRC + sl;
+        if (sn < A.npsrc) {
+          const double* pn = A.phi + (size_t(t) * A.nsrc + sn) * A.na;
+          if (lane < A.na) tc::prefetch_l1(pn + lane);
+          if (lane + 32 < A.na) tc::prefetch_l1(pn + lane + 32);
+          if (lane == 0) {
+            tc::prefetch_l1(A.lm + 2 * sn);
+            if (A.bsq0) tc::prefetch_l1(A.bsq0 + kBsqVals * (size_t(sn) * A.ntime + t));
+          }
+        }
+      }
       if (!bad) bad = !tc::mbar_wait(empty + slot, (use & 1) ^ 1, wlim);
       if (!bad) {
-        const int s0 = g * NSRC, ns = min(NSRC, A.npsrc - s0);
         unsigned char* hi = stage + size_t(slot) * 2 * L::kMatBytes;
         unsigned char* lo = hi + L::kMatBytes;
         // the source's terms, the same for both antennas of the lane
@@ -832,14 +844,24 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
         tc::fence_proxy_async_smem();
         tc::mbar_arrive(full + slot);
       }
-      if ((g % group) == group - 1 || g == nstages - 1) {
-        if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1, wlim);
+      // A group is drained once the first stage of the next one is staged,
+      // so the group's last MMAs run while the warps produce that stage.
+      if ((g % group) == 0 && g > 0) {
+        if (!bad) bad = !tc::mbar_wait(accfull, ((g / group) - 1) & 1, wlim);
         tc::fence_after_thread_sync();
         bad = __any_sync(0xffffffffu, bad);  // the drain's TMEM loads are warp-collective
-        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), g < nstages - 1);
+        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), true);
         tc::fence_before_thread_sync();
         if (!bad) tc::mbar_arrive(accfree);
       }
+    }
+    if (nstages > 0) {  // the last group
+      if (!bad) bad = !tc::mbar_wait(accfull, ((nstages - 1) / group) & 1, wlim);
+      tc::fence_after_thread_sync();
+      bad = __any_sync(0xffffffffu, bad);
+      if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), false);
+      tc::fence_before_thread_sync();
+      if (!bad) tc::mbar_arrive(accfree);
     }
   } else {
     // ---- MMA issue (lane 0); the whole warp drains with the producers ------
@@ -850,6 +872,14 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
     for (int g = 0; g < nstages; ++g) {
       const int slot = g % kTcStages, use = g / kTcStages;
       const bool first = (g % group) == 0, last = (g % group) == group - 1 || g == nstages - 1;
+      if (first && g > 0) {  // the previous group, as the producers drain it
+        if (!bad) bad = !tc::mbar_wait(accfull, ((g / group) - 1) & 1, wlim);
+        tc::fence_after_thread_sync();
+        bad = __any_sync(0xffffffffu, bad);
+        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), true);
+        tc::fence_before_thread_sync();
+        if (!bad) tc::mbar_arrive(accfree);
+      }
       if (lane == 0 && !bad) {
         if (first && g > 0) {
           bad = !tc::mbar_wait(accfree, ((g / group) - 1) & 1, wlim);
@@ -893,14 +923,15 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
           if (last) tc::mma_commit(accfull);
         }
       }
-      if (last) {
-        if (!bad) bad = !tc::mbar_wait(accfull, (g / group) & 1, wlim);
-        tc::fence_after_thread_sync();
-        bad = __any_sync(0xffffffffu, bad);
-        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), g < nstages - 1);
-        tc::fence_before_thread_sync();
-        if (!bad) tc::mbar_arrive(accfree);
-      }
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    if (nstages > 0) {  // the last group
+      if (!bad) bad = !tc::mbar_wait(accfull, ((nstages - 1) / group) & 1, wlim);
+      tc::fence_after_thread_sync();
+      bad = __any_sync(0xffffffffu, bad);
+      if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), false);
+      tc::fence_before_thread_sync();
+      if (!bad) tc::mbar_arrive(accfree);
     }
     if (lane == 0 && issued) {  // all MMAs finished before TMEM is released
       tc::mma_commit(done);
@@ -1066,86 +1097,31 @@ __device__ void beam_interp_d(const T* __restrict__ E_beam, const BeamGeom& G, c
   }
 }
 
-// Same as beam_interp_d on the frequency-blended plane (4 corners).  In
-// FP32 each of the 12 plane values is interpolated in the difference form
-//   f = f00 + x (f10 - f00) + y (b + x c),  b = f01 - f00,
-//   c = f11 - f10 - b,  df/dx = (f10 - f00) + y c,  df/dy = b + x c,
-// the same bilinear function and derivatives with fewer operations.
+// Same as beam_interp_d on the frequency-blended coefficient plane (see
+// plane_cell): the bilinear values and their derivatives along the l and m
+// grid axes, then the renormalisation and its derivatives.
 template <typename T>
 __device__ void beam_interp_plane_d(const T* __restrict__ plane, int mh, const GridPos<T>& gl, const GridPos<T>& gm,
                                     Jones<T>& E, Jones<T>& dEl, Jones<T>& dEm) {
-  Jones<T> sum = jzero<T>(), dsl = jzero<T>(), dsm = jzero<T>();
-  T amp[4] = {0, 0, 0, 0}, dal[4] = {0, 0, 0, 0}, dam[4] = {0, 0, 0, 0};
-  const T ld = gl.d, md = gm.d;
-  if constexpr (sizeof(T) == 4) {
-    const float4* p00 = reinterpret_cast<const float4*>(plane + kPlaneVals * (size_t(gl.i0) * mh + gm.i0));
-    const float4* p10 = reinterpret_cast<const float4*>(plane + kPlaneVals * (size_t(gl.i1) * mh + gm.i0));
-    const float4* p01 = reinterpret_cast<const float4*>(plane + kPlaneVals * (size_t(gl.i0) * mh + gm.i1));
-    const float4* p11 = reinterpret_cast<const float4*>(plane + kPlaneVals * (size_t(gl.i1) * mh + gm.i1));
-    float* sv = reinterpret_cast<float*>(&sum);
-    float* lv = reinterpret_cast<float*>(&dsl);
-    float* mv = reinterpret_cast<float*>(&dsm);
-#pragma unroll
-    for (int v = 0; v < 3; ++v) {  // float4 runs: E.a E.b | E.c E.d | |E|
-      const float4 q00 = __ldg(p00 + v), q10 = __ldg(p10 + v), q01 = __ldg(p01 + v), q11 = __ldg(p11 + v);
-      const float f00[4] = {q00.x, q00.y, q00.z, q00.w}, f10[4] = {q10.x, q10.y, q10.z, q10.w};
-      const float f01[4] = {q01.x, q01.y, q01.z, q01.w}, f11[4] = {q11.x, q11.y, q11.z, q11.w};
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float a = f10[k] - f00[k], b = f01[k] - f00[k], c = f11[k] - f10[k] - b;
-        const float fy = fmaf(ld, c, b), fx = fmaf(md, c, a);
-        const float fv = fmaf(md, fy, fmaf(ld, a, f00[k]));
-        if (v < 2) {
-          sv[4 * v + k] = fv; lv[4 * v + k] = fx; mv[4 * v + k] = fy;
-        } else {
-          amp[k] = fv; dal[k] = fx; dam[k] = fy;
-        }
-      }
-    }
-  } else {
-#pragma unroll
-  for (int corner = 0; corner < 4; ++corner) {
-    const bool hl = corner & 1, hm = corner & 2;
-    const int il = hl ? gl.i1 : gl.i0, im = hm ? gm.i1 : gm.i0;
-    const T fl = hl ? ld : T(1) - ld, fm = hm ? md : T(1) - md;
-    const T w = fl * fm, wl = (hl ? T(1) : T(-1)) * fm, wm = fl * (hm ? T(1) : T(-1));
-    const T* p = plane + kPlaneVals * (size_t(il) * mh + im);
-    Jones<T> e = jldg<T>(p);
-    T abv[4];
-    if constexpr (sizeof(T) == 4) {  // 48-byte entries: |E| starts 16-byte aligned
-      const float4 q = __ldg(reinterpret_cast<const float4*>(p + 8));
-      abv[0] = q.x; abv[1] = q.y; abv[2] = q.z; abv[3] = q.w;
-    } else {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) abv[k] = __ldg(p + 8 + k);
-    }
-    const Cx<T>* e4 = &e.a;
-    Cx<T>* s4 = &sum.a; Cx<T>* l4 = &dsl.a; Cx<T>* m4 = &dsm.a;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const T ab = abv[k];
-      s4[k] = s4[k] + e4[k] * w; amp[k] += w * ab;
-      l4[k] = l4[k] + e4[k] * wl; dal[k] += wl * ab;
-      m4[k] = m4[k] + e4[k] * wm; dam[k] += wm * ab;
-    }
-  }
-  }
+  T v[kPlaneComp], vx[kPlaneComp], vy[kPlaneComp];
+  plane_cell<T, true>(plane_cell_ptr(plane, mh, gl.i0, gm.i0), gl.d, gm.d, v, vx, vy);
   // E = s g with g = amp / |s|, and by the quotient rule
   //   dE/dx = g ds/dx + s inv (damp/dx - g inv Re(conj(s) ds/dx)),  inv = 1 / |s|;
   // a non-finite inv (s = 0) is replaced by 1, which gives the same value as
   // leaving out the normalisation (E = s amp, dE/dx = ds/dx amp + s damp/dx).
   Cx<T>* E4 = &E.a; Cx<T>* dl4 = &dEl.a; Cx<T>* dm4 = &dEm.a;
-  const Cx<T>* s4 = &sum.a; const Cx<T>* l4 = &dsl.a; const Cx<T>* m4 = &dsm.a;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    T inv = mb_rsqrt(s4[k].r * s4[k].r + s4[k].i * s4[k].i);
+    const Cx<T> s4{v[2 * k], v[2 * k + 1]}, l4{vx[2 * k], vx[2 * k + 1]}, m4{vy[2 * k], vy[2 * k + 1]};
+    const T amp = v[8 + k], dal = vx[8 + k], dam = vy[8 + k];
+    T inv = mb_rsqrt(s4.r * s4.r + s4.i * s4.i);
     inv = isfinite(inv) ? inv : T(1);
-    const T g = amp[k] * inv, gi = g * inv;
-    E4[k] = s4[k] * g;
-    const T hl = inv * (dal[k] - gi * cdot_re(s4[k], l4[k]));
-    const T hm = inv * (dam[k] - gi * cdot_re(s4[k], m4[k]));
-    dl4[k] = {l4[k].r * g + s4[k].r * hl, l4[k].i * g + s4[k].i * hl};
-    dm4[k] = {m4[k].r * g + s4[k].r * hm, m4[k].i * g + s4[k].i * hm};
+    const T g = amp * inv, gi = g * inv;
+    E4[k] = s4 * g;
+    const T hl = inv * (dal - gi * cdot_re(s4, l4));
+    const T hm = inv * (dam - gi * cdot_re(s4, m4));
+    dl4[k] = {l4.r * g + s4.r * hl, l4.i * g + s4.i * hl};
+    dm4[k] = {m4.r * g + s4.r * hm, m4.i * g + s4.i * hm};
   }
 }
 
@@ -1467,10 +1443,10 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
 // that take alternate tiles.  Worker lane (a, i) = TMEM lane 2a + i handles
 // the items (source 4i + u, antenna a), u = 0..3, of its group's tile: it
 // computes E, dE/dl, dE/dm, K and J once, stages J for the MMA and parks
-//   EK = E K,  Pl = dE/dl (K sqrt(B)),  Pm = dE/dm (K sqrt(B))
+//   EK = E K,  DL = dE/dl K,  DM = dE/dm K
 // in shared memory (6 float4 per item) until dJ arrives in TMEM.
-// Then, with gJ = dJ,
-//   d sqrt(B) = EK^H gJ,  d/dl_beam = Re tr(gJ^H Pl),  d/dm_beam = Re tr(gJ^H Pm),
+// Then, with gJ = dJ and W = gJ sqrt(B),
+//   d sqrt(B) = EK^H gJ,  d/dl_beam = Re tr(W^H DL),  d/dm_beam = Re tr(W^H DM),
 //   d/dphi = 2 pi nu / c * Im tr(d sqrt(B)^H sqrt(B)).
 // Lane 0 of the group's first and second warps issue the Re and Im MMA
 // chains once the group has staged its tile (group barrier); while one group
@@ -1759,17 +1735,18 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
           Jones<float> E, dEl, dEm;
           if (plane) beam_interp_plane_d<float>(plane, A.mh, gl, gm, E, dEl, dEm);
           else beam_interp_d<float>(A.E_beam, G, gl, gm, cp, E, dEl, dEm);
-          const Jones<float> B = {{tb.x, 0.f}, {tb.z, tb.w}, {tb.z, -tb.w}, {tb.y, 0.f}};
-          const Jones<float> KB = {cmul(K, B.a), cmul(K, B.b), cmul(K, B.c), cmul(K, B.d)};
-          J = jmul(E, KB);
+          // J = (E K) sqrt(B); the beam derivatives are parked times K (zero
+          // where the grid coordinate was clamped), sqrt(B) joins in the chain
           const Jones<float> EK = {cmul(E.a, K), cmul(E.b, K), cmul(E.c, K), cmul(E.d, K)};
-          const Jones<float> Pl = jscale(jmul(dEl, KB), gl.inside ? A.lscale : 0.f);
-          const Jones<float> Pm = jscale(jmul(dEm, KB), gm.inside ? A.mscale : 0.f);
+          J = jmul_herm_real_diag(EK, tb.x, tb.y, Cx<float>{tb.z, tb.w});
+          const Cx<float> Kl = gl.inside ? K : Cx<float>{0.f, 0.f}, Km = gm.inside ? K : Cx<float>{0.f, 0.f};
+          const Jones<float> DL = {cmul(dEl.a, Kl), cmul(dEl.b, Kl), cmul(dEl.c, Kl), cmul(dEl.d, Kl)};
+          const Jones<float> DM = {cmul(dEm.a, Km), cmul(dEm.b, Km), cmul(dEm.c, Km), cmul(dEm.d, Km)};
 #pragma unroll
           for (int e = 0; e < 8; ++e) {
             st[0][e] = reinterpret_cast<const float*>(&EK)[e];
-            st[1][e] = reinterpret_cast<const float*>(&Pl)[e];
-            st[2][e] = reinterpret_cast<const float*>(&Pm)[e];
+            st[1][e] = reinterpret_cast<const float*>(&DL)[e];
+            st[2][e] = reinterpret_cast<const float*>(&DM)[e];
           }
         }
         // park the item's state in shared memory (lane-contiguous float4)
@@ -1839,7 +1816,7 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
         float gsum[8];  // kTaAcc values, zero padded for the reduce-scatter
 #pragma unroll
         for (int e = 0; e < 8; ++e) gsum[e] = 0.f;
-        float sv[24];  // parked EK, Pl, Pm of the item
+        float sv[24];  // parked EK, DL, DM of the item
 #pragma unroll
         for (int x = 0; x < kTaPark; ++x) {
           const float4 p4 = mypark[(u * kTaPark + x) * 128];
@@ -1847,15 +1824,17 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
         }
         if (!bad && ant_ok && sl < ns) {
           const float4 tb = tsrc[sl].b, tlm = tsrc[sl].lm;
-          Jones<float> EK, Pl, Pm;
+          Jones<float> EK, DL, DM;
 #pragma unroll
           for (int e = 0; e < 8; ++e) {
             reinterpret_cast<float*>(&EK)[e] = sv[e];
-            reinterpret_cast<float*>(&Pl)[e] = sv[8 + e];
-            reinterpret_cast<float*>(&Pm)[e] = sv[16 + e];
+            reinterpret_cast<float*>(&DL)[e] = sv[8 + e];
+            reinterpret_cast<float*>(&DM)[e] = sv[16 + e];
           }
           const Jones<float> gB = jhmul(EK, gJ);
-          const float g_ld = jdot_re(gJ, Pl), g_md = jdot_re(gJ, Pm);
+          // Re tr(gJ^H dE K sqrt(B)) = Re tr((gJ sqrt(B))^H dE K), sqrt(B) Hermitian
+          const Jones<float> W = jmul_herm_real_diag(gJ, tb.x, tb.y, Cx<float>{tb.z, tb.w});
+          const float g_ld = A.lscale * jdot_re(W, DL), g_md = A.mscale * jdot_re(W, DM);
           // Im tr(gB^H B), B = [[a, b], [conj(b), d]] with a, d real
           const float imt = -gB.a.i * tb.x - gB.d.i * tb.y + (gB.b.r * tb.w - gB.b.i * tb.z) -
                             (gB.c.r * tb.w + gB.c.i * tb.z);
@@ -1916,7 +1895,8 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
 // ---------------------------------------------------------------------------
 // Small kernels: FP64 phase path lengths, gradient finalisation
 // ---------------------------------------------------------------------------
-// Frequency-blended beam plane per active channel (see beam_interp_plane).
+// Frequency-blended beam plane per active channel as bilinear coefficients
+// per (l, m) cell (see plane_cell), formed in FP64 from the cube.
 template <typename T>
 __global__ void beam_plane_kernel(FusedArgs<T> A, T* __restrict__ plane) {
   const size_t cells = size_t(A.lw) * A.mh;
@@ -1924,16 +1904,33 @@ __global__ void beam_plane_kernel(FusedArgs<T> A, T* __restrict__ plane) {
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
     const int ch = int(i / cells);
     const size_t cell = i - size_t(ch) * cells;
+    const int il = int(cell / A.mh), im = int(cell % A.mh);
+    const int il1 = min(il + 1, A.lw - 1), im1 = min(im + 1, A.mh - 1);
     const ChanPos<T> cp = chan_pos<T>(A.freq[ch], A.lfreq, A.ufreq, A.nud);
-    const T* e0 = A.E_beam + 8 * (cell * A.nud + cp.c0);
-    const T* e1 = A.E_beam + 8 * (cell * A.nud + cp.c1);
-    T* out = plane + kPlaneVals * i;
-    const T w0 = T(1) - cp.d, w1 = cp.d;
+    const double w0 = 1.0 - double(cp.d), w1 = double(cp.d);
+    double v[4][kPlaneComp];  // corners (il, im), (il1, im), (il, im1), (il1, im1)
+    const int cl[4] = {il, il1, il, il1}, cm[4] = {im, im, im1, im1};
+#pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const Cx<T> a{e0[2 * k], e0[2 * k + 1]}, b{e1[2 * k], e1[2 * k + 1]};
-      out[2 * k] = w0 * a.r + w1 * b.r;
-      out[2 * k + 1] = w0 * a.i + w1 * b.i;
-      out[8 + k] = w0 * cabs_(a) + w1 * cabs_(b);
+      const size_t c = size_t(cl[k]) * A.mh + cm[k];
+      const T* e0 = A.E_beam + 8 * (c * A.nud + cp.c0);
+      const T* e1 = A.E_beam + 8 * (c * A.nud + cp.c1);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double ar = e0[2 * q], ai = e0[2 * q + 1], br = e1[2 * q], bi = e1[2 * q + 1];
+        v[k][2 * q] = w0 * ar + w1 * br;
+        v[k][2 * q + 1] = w0 * ai + w1 * bi;
+        v[k][8 + q] = w0 * sqrt(ar * ar + ai * ai) + w1 * sqrt(br * br + bi * bi);
+      }
+    }
+    T* out = plane + kPlaneVals * i;
+#pragma unroll
+    for (int q = 0; q < kPlaneComp; ++q) {
+      const double b = v[2][q] - v[0][q];
+      out[q] = T(v[0][q]);
+      out[kPlaneComp + q] = T(v[1][q] - v[0][q]);
+      out[2 * kPlaneComp + q] = T(b);
+      out[3 * kPlaneComp + q] = T(v[3][q] - v[1][q] - b);
     }
   }
 }
