@@ -145,3 +145,43 @@ def test_parallactic_angles_shape_and_transit():
     ra_d, dec_d = util.precess_j2000(fc[0], fc[1], times)
     ha = util.gmst(times) - ra_d
     np.testing.assert_allclose(pa[:, 0], util.parallactic_angle(ha, dec_d, 0.0), atol=1e-12)
+
+
+def test_parallactic_angle_error_from_omitted_terms():
+    """Moving the direction by the summed omitted terms (nutation,
+    aberration, UT1 - UTC, polar motion: 60.9" = 2.95e-4 rad) changes the
+    parallactic angle by no more than e (tan(elevation) + |tan(dec)|).  For
+    the generator's field (dec -30 deg) at elevations up to 60 degrees that
+    is 6.8e-4 rad, which moves a source 0.07 rad from the field centre by
+    4.8e-5 rad on the beam and changes the synthetic 50 x 50 x 32 beam's E
+    by at most 1.5e-3 of its largest value (5e-5 norm-wise over the sources
+    of the test sky)."""
+    from montblanc_gb300 import util, synth
+    from oracle import rime_v4 as O
+    e = util.omitted_direction_error()
+    assert abs(e - 60.89762 * util.ARCSEC) < 1e-12
+    lat = np.deg2rad(-30.0)
+    rng = np.random.default_rng(3)
+    for _ in range(4000):
+        H = rng.uniform(-np.pi, np.pi)
+        dec = rng.uniform(-np.deg2rad(80.0), np.deg2rad(80.0))
+        sin_el = np.sin(lat) * np.sin(dec) + np.cos(lat) * np.cos(dec) * np.cos(H)
+        el = np.arcsin(sin_el)
+        if not (0.0 < el <= np.deg2rad(80.0)):
+            continue
+        chi = util.parallactic_angle(H, dec, lat)
+        bound = util.parallactic_angle_error_bound(el, dec)
+        for ang in np.linspace(0, 2 * np.pi, 8, endpoint=False):  # displacement by e in any direction
+            dH, dd = e * np.cos(ang) / np.cos(dec), e * np.sin(ang)
+            d = np.angle(np.exp(1j * (util.parallactic_angle(H + dH, dec + dd, lat) - chi)))
+            assert abs(d) <= 1.02 * bound + 1e-12, (np.rad2deg(el), np.rad2deg(dec), d, bound)
+    field = float(util.parallactic_angle_error_bound(np.deg2rad(60.0), np.deg2rad(-30.0)))
+    assert 6.7e-4 < field < 6.9e-4
+    # its effect on E for the synthetic beam and the sky of the test workloads
+    P = synth.make_problem(ntime=2, na=3, nchan=2, npsrc=200, seed=5)
+    E0 = O.e_beam(P)
+    P['parallactic_angles'] = P['parallactic_angles'] + field
+    E1 = O.e_beam(P)
+    rel = np.max(np.abs(E1 - E0)) / np.max(np.abs(E0))
+    assert rel < 1.5e-3, rel
+    assert np.linalg.norm(E1 - E0) / np.linalg.norm(E0) < 6e-5
