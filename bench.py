@@ -48,13 +48,13 @@ NCU_LIMITER = {
     'coh_tc_adj_kernel': {
         'source': 'profiles/coh_tc_adj_kernel_profile_point.md',
         'limiter': 'CUDA-core issue and latency of the per-(source, antenna) producer and chain',
-        'sm__pipe_tensor_cycles_active': 0.097, 'smsp__issue_active': 0.448,
-        'pipe_fma': 0.261, 'pipe_alu': 0.245, 'pipe_fp64': 0.055, 'pipe_xu': 0.042},
+        'sm__pipe_tensor_cycles_active': 0.103, 'smsp__issue_active': 0.421,
+        'pipe_fma': 0.220, 'pipe_alu': 0.262, 'pipe_fp64': 0.058, 'pipe_xu': 0.044},
     'coh_tc_fwd_kernel': {
         'source': 'profiles/coh_tc_fwd_kernel_profile_point.md',
         'limiter': 'CUDA-core issue and latency of the per-(source, antenna) producer; TMEM drains',
-        'sm__pipe_tensor_cycles_active': 0.281, 'smsp__issue_active': 0.438,
-        'pipe_fma': 0.192, 'pipe_alu': 0.329, 'pipe_fp64': 0.070, 'pipe_xu': 0.038},
+        'sm__pipe_tensor_cycles_active': 0.302, 'smsp__issue_active': 0.452,
+        'pipe_fma': 0.184, 'pipe_alu': 0.352, 'pipe_fp64': 0.074, 'pipe_xu': 0.041},
 }
 
 # DRAM bytes per launch from a one-kernel ncu capture on the profile_point
