@@ -307,9 +307,10 @@ def batched_likelihood(seed, nsets=256, reps=2):
     """256 parameter sets (per-set source counts log-uniform in 10..5000,
     point / gaussian / sersic mix) against one 100 x 27 x 64 observation:
     chi^2 + gradient of every set per batch, the form and source tile
-    autotuned per set,
-    the batch captured as one CUDA graph and replayed.  Errors against the
-    FP64 form on the smallest, median and largest sets."""
+    autotuned per set, all sets of a form in one forward and one adjoint
+    launch (mb_rime_batch), the batch captured as one CUDA graph and
+    replayed.  Errors against the FP64 form on the smallest, median and
+    largest sets."""
     import numpy as np
     import torch
     from montblanc_gb300 import synth
@@ -333,6 +334,11 @@ def batched_likelihood(seed, nsets=256, reps=2):
     b.capture()
     b.run()
     torch.cuda.synchronize()
+    from montblanc_gb300 import _cabi
+    l0 = _cabi.lib.mb_kernel_launches()
+    b.enqueue()
+    torch.cuda.synchronize()
+    launches = int(_cabi.lib.mb_kernel_launches() - l0)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(reps):
@@ -356,7 +362,10 @@ def batched_likelihood(seed, nsets=256, reps=2):
     return {'workload': '%d sets x (ntime 100, na 27, nchan 64), per-set nsrc log-uniform 10..5000 '
                         '(%d sources in all), shared observation' % (nsets, int(n.sum())),
             'sets_per_s': nsets / (ms * 1e-3), 'terms_per_s': b.terms() / (ms * 1e-3), 'ms_per_batch': ms,
-            'execution': 'one CUDA graph replay per batch (forward + adjoint of every set)',
+            'execution': 'one CUDA graph replay per batch of %d kernel launches: shared tables, one forward and '
+                         'one adjoint launch per (form, source tile) over all its sets\' (time, channel) units, '
+                         'the chi^2 sums, the gradients' % launches,
+            'launches_per_batch': launches,
             'forms': {f: forms.count(f) for f in set(forms)},
             'choices': {'%s/%d' % c: n_c for c, n_c in
                         ((c, list(zip(b.forms, b.tiles)).count(c)) for c in set(zip(b.forms, b.tiles)))},

@@ -242,6 +242,58 @@ mb_status mb_rime_status(mb_dtype dtype, mb_mode mode, const mb_dims* dims,
                          int want_grad, const void* workspace,
                          size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Batched likelihood.  No counterpart in the reference: it solves one
+ * resident problem per solver; its closest caller is the v5 driver's
+ * per-chunk enqueue (impl/rime/v5/CompositeRimeSolver.py:925-975).
+ *
+ * chi^2 and its gradient for nsets parameter sets (sampler proposals)
+ * against one observation.  Every input of mb_rime_inputs except the source
+ * arrays (lm, stokes, alpha, gauss_shape, sersic_shape, which are ignored)
+ * is shared; each set brings its own source counts, source arrays (stokes
+ * and alpha with the observation's local time size as row stride, shapes as
+ * (3, n) with n its own count) and gradient outputs.  The source dimensions
+ * of `dims` are ignored.  All sets of one kernel form (mode and source tile)
+ * run as one forward launch and one adjoint launch whose CTAs are the sets'
+ * (time, channel) units, largest sets first, so a call launches a fixed
+ * handful of kernels however many sets it holds.
+ * ---------------------------------------------------------------------- */
+typedef struct mb_batch_set {
+  uint32_t npsrc, ngsrc, nssrc;
+  uint32_t mode;      /* mb_mode of this set's kernels (split modes: FLOAT32) */
+  uint32_t options;   /* MB_SOURCE_TILE_* bits of this set's CUDA-core kernels, or 0 */
+  uint32_t reserved;  /* 0 */
+  const void* lm;           /* (nsrc, 2) */
+  const void* stokes;       /* (nsrc, ntime, 4) */
+  const void* alpha;        /* (nsrc, ntime) */
+  const void* gauss_shape;  /* (3, ngsrc), NULL if ngsrc == 0 */
+  const void* sersic_shape; /* (3, nssrc), NULL if nssrc == 0 */
+  mb_rime_grads grads;      /* this set's gradient outputs, any may be NULL */
+} mb_batch_set;
+
+/* Workspace bytes of a batch (per set: FP64 path lengths, d chi^2 / dV,
+ * d chi^2 / dG and accumulators), or 0 if the arguments are invalid. */
+size_t mb_rime_batch_workspace_size(mb_dtype dtype, const mb_dims* dims,
+                                    const mb_batch_set* sets, int nsets);
+
+/* Writes the per-set table and the launches' (set, unit) lists into the
+ * workspace; synchronises `stream`.  Call it again after changing any set's
+ * counts, mode, options, arrays or outputs; not capturable in a CUDA graph. */
+mb_status mb_rime_batch_prepare(mb_dtype dtype, const mb_dims* dims,
+                                const mb_batch_set* sets, int nsets,
+                                void* workspace, size_t workspace_bytes,
+                                void* stream);
+
+/* chi^2 of every set into X2[0 .. nsets) (device doubles, divided by
+ * sigma_sqrd when weights are off) and grad_scale * d chi^2 / d(parameters)
+ * into each set's outputs, from the tables mb_rime_batch_prepare wrote for
+ * the same `sets`.  Stream-ordered, allocates nothing, capturable. */
+mb_status mb_rime_batch(mb_dtype dtype, const mb_dims* dims,
+                        const mb_props* props, uint32_t options,
+                        const mb_rime_inputs* shared, const mb_batch_set* sets,
+                        int nsets, double* X2, double grad_scale,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
 /* Diagnostic, no counterpart in the reference: the poll limit of the
  * pipeline waits of the tensor-core kernels on the current device (default
  * mb_default_wait_limit() = 2^20).  0 makes every such wait give up at once,

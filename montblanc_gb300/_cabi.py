@@ -73,6 +73,13 @@ class MbRimeGrads(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in GRAD_NAMES]
 
 
+class MbBatchSet(ctypes.Structure):
+    _fields_ = [('npsrc', ctypes.c_uint32), ('ngsrc', ctypes.c_uint32), ('nssrc', ctypes.c_uint32),
+                ('mode', ctypes.c_uint32), ('options', ctypes.c_uint32), ('reserved', ctypes.c_uint32),
+                ('lm', ctypes.c_void_p), ('stokes', ctypes.c_void_p), ('alpha', ctypes.c_void_p),
+                ('gauss_shape', ctypes.c_void_p), ('sersic_shape', ctypes.c_void_p), ('grads', MbRimeGrads)]
+
+
 # (name, restype, argtypes) of every exported function.
 _vp, _sz, _u32, _i32, _dbl = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_int, ctypes.c_double
 _pdims, _pprops = ctypes.POINTER(MbDims), ctypes.POINTER(MbProps)
@@ -93,6 +100,10 @@ SIGNATURES = {
     'mb_rime_adjoint': (_i32, [_i32, _i32, _pdims, _pprops, _u32, ctypes.POINTER(MbRimeInputs), _dbl,
                                ctypes.POINTER(MbRimeGrads), _vp, _sz, _vp]),
     'mb_rime_status': (_i32, [_i32, _i32, _pdims, _i32, _vp, _sz, _vp]),
+    'mb_rime_batch_workspace_size': (_sz, [_i32, _pdims, ctypes.POINTER(MbBatchSet), _i32]),
+    'mb_rime_batch_prepare': (_i32, [_i32, _pdims, ctypes.POINTER(MbBatchSet), _i32, _vp, _sz, _vp]),
+    'mb_rime_batch': (_i32, [_i32, _pdims, _pprops, _u32, ctypes.POINTER(MbRimeInputs),
+                             ctypes.POINTER(MbBatchSet), _i32, _vp, _dbl, _vp, _sz, _vp]),
     'mb_set_wait_limit': (_i32, [_u32]),
     'mb_default_wait_limit': (_u32, []),
     'mb_tc_selftest': (_i32, [_vp, _vp, _i32, _i32, _vp, _vp, _vp]),

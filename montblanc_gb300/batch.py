@@ -6,9 +6,12 @@ observation (uvw, antenna pairs, frequencies, beam, pointing, G, flags,
 weights, observed visibilities) and differs only in its sources (lm,
 Stokes, alpha, shapes), with its own source counts.  ``RimeBatch`` keeps the
 observation on the device once, the sets' parameters in concatenated device
-arrays, and evaluates every set's chi^2 and gradient as one CUDA graph: the
-per-set ``mb_rime_forward`` / ``mb_rime_adjoint`` sequence is captured once
-and replayed, so a batch costs one graph launch.
+arrays, and evaluates every set's chi^2 and gradient with ``mb_rime_batch``:
+all sets of one kernel form run as one forward launch and one adjoint
+launch whose CTAs are the sets' (time, channel) units (largest sets first),
+so a batch is a fixed handful of launches (shared tables, one forward and
+one adjoint per (form, source tile), the chi^2 sums, the gradients), which
+``capture`` records once as a CUDA graph and ``run`` replays.
 
 The kernel form of each set (CUDA-core ``native`` or tensor-core
 ``split_tf32``) and the source tile of its CUDA-core kernels (sources per
@@ -118,7 +121,9 @@ class RimeBatch(object):
         self.forms = ['split_tf32' if dtype == 'float' else 'native'] * self.nsets
         self.tiles = [0] * self.nsets
         self._graph = None
-        self._ws = None
+        self._ws = None        # single-set workspace (autotuner timings)
+        self._bws = None       # batch workspace
+        self._prepared = None  # (forms, tiles) the batch workspace's tables were written for
 
     # ---- per-set call arguments -------------------------------------------------
     def _dims(self, i):
@@ -185,10 +190,55 @@ class RimeBatch(object):
         _cabi.call('mb_rime_adjoint', self.mb_dtype, mode, ctypes.byref(d), ctypes.byref(props), self._options(i),
                    ctypes.byref(inp), 1.0, ctypes.byref(g), ptr(ws), ws.numel(), handle)
 
-    def enqueue(self, stream=None):
-        self.workspace()
+    # ---- the batched call ---------------------------------------------------------
+    def _batch_sets(self):
+        arr = (_cabi.MbBatchSet * max(self.nsets, 1))()
         for i in range(self.nsets):
-            self.enqueue_set(i, stream)
+            npt, ng, ns = self.counts[i]
+            b = arr[i]
+            b.npsrc, b.ngsrc, b.nssrc = npt, ng, ns
+            b.mode = _cabi.MODES[self.forms[i]]
+            b.options = _cabi.source_tile_bits(self.tiles[i]) if self.tiles[i] else 0
+            b.reserved = 0
+            p = self._set_ptrs(self.params, i)
+            b.lm, b.stokes, b.alpha = p['lm'], p['stokes'], p['alpha']
+            b.gauss_shape, b.sersic_shape = p['gauss_shape'], p['sersic_shape']
+            b.grads = self._grad_struct(i)
+        return arr
+
+    def prepare(self, stream=None):
+        """Size the batch workspace and write its per-set table and launch
+        lists (synchronous; done again only when forms or tiles change)."""
+        key = (tuple(self.forms), tuple(self.tiles))
+        if self._prepared == key:
+            return
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        self._sets_c = self._batch_sets()
+        d = self._dims(0) if self.nsets else _cabi.make_dims(self.ntime, self.na, self.nbl, self.nchan, 0,
+                                                             beam=self.beam)
+        self._obs_dims = d
+        need = _cabi.lib.mb_rime_batch_workspace_size(self.mb_dtype, ctypes.byref(d), self._sets_c, self.nsets)
+        if need == 0 and self.nsets:
+            raise _cabi.MontblancError(_cabi.MB_ERR_INVALID_ARG, 'mb_rime_batch_workspace_size',
+                                       _cabi.lib.mb_last_error_string().decode())
+        if self._bws is None or self._bws.numel() < need:
+            self._bws = None
+            self._bws = torch.empty(max(need, 256), dtype=torch.uint8, device=self.device)
+        _cabi.call('mb_rime_batch_prepare', self.mb_dtype, ctypes.byref(d), self._sets_c, self.nsets,
+                   ptr(self._bws), self._bws.numel(), ctypes.c_void_p(s.cuda_stream))
+        self._inputs_c = self._inputs(0) if self.nsets else None
+        self._props_c = _cabi.make_props(**self.props)
+        self._prepared = key
+
+    def enqueue(self, stream=None):
+        """chi^2 (into X2) and gradients of every set: one mb_rime_batch call."""
+        self.prepare(stream)
+        if self.nsets == 0:
+            return
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _cabi.call('mb_rime_batch', self.mb_dtype, ctypes.byref(self._obs_dims), ctypes.byref(self._props_c),
+                   self._options(), ctypes.byref(self._inputs_c), self._sets_c, self.nsets, ptr(self.X2), 1.0,
+                   ptr(self._bws), self._bws.numel(), ctypes.c_void_p(s.cuda_stream))
 
     # ---- tuning and graphs -------------------------------------------------------------
     def _time_set(self, i, form, reps, tile=0):
@@ -243,7 +293,7 @@ class RimeBatch(object):
 
     def capture(self):
         """Capture the whole batch as one CUDA graph (forms fixed)."""
-        self.workspace()
+        self.prepare()
         torch.cuda.synchronize(self.device)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, capture_error_mode='relaxed'):

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <mutex>
+#include <vector>
 
 #include "mb_fused.h"
 #include "mb_tc_layout.cuh"
@@ -151,6 +152,32 @@ __device__ __forceinline__ const Jones<T>* jtile(const Jones<T>* base, const Sme
 // ---------------------------------------------------------------------------
 // Shared set-up and producer
 // ---------------------------------------------------------------------------
+// Batched launches: the parameter set a CTA works on replaces the single
+// problem's per-set fields of A (source counts and arrays, tables, partials,
+// the forward's d chi^2 / dV and d chi^2 / dG, the FP64 accumulators).  A
+// negative sbeg (the extended sources' adjoint of tensor-core sets) becomes
+// the set's point-source count.
+template <typename T>
+__device__ __forceinline__ void use_set(FusedArgs<T>& A, const BatchSet<T>& b) {
+  A.lm = b.lm; A.stokes = b.stokes; A.alpha = b.alpha; A.gauss = b.gauss; A.sersic = b.sersic;
+  A.npsrc = b.npsrc; A.ngsrc = b.ngsrc; A.nssrc = b.nssrc; A.nsrc = b.npsrc + b.ngsrc + b.nssrc;
+  A.lgsrc = b.ngsrc; A.lssrc = b.nssrc;
+  A.phi = b.phi; A.bsq0 = b.bsq0; A.partial = b.partial; A.gV = b.gV; A.dG = b.dG;
+  A.acc_lm = b.acc_lm; A.acc_stokes = b.acc_stokes; A.acc_alpha = b.acc_alpha;
+  A.acc_gauss = b.acc_gauss; A.acc_sersic = b.acc_sersic;
+  if (A.sbeg < 0) A.sbeg = b.npsrc;
+}
+
+// The (time, channel) unit of this CTA: blockIdx.x for a single problem;
+// in a batched launch the CTA's (set, unit) item, whose set it selects.
+template <typename T>
+__device__ __forceinline__ int cta_unit(FusedArgs<T>& A) {
+  if (A.bitems == nullptr) return blockIdx.x;
+  const int2 it = A.bitems[blockIdx.x];
+  use_set(A, A.bsets[it.x]);
+  return it.y;
+}
+
 template <typename T>
 __device__ void load_antennas(const FusedArgs<T>& A, int t, int ch, AntInfo<T>* sa) {
   for (int a = threadIdx.x; a < A.na; a += blockDim.x) {
@@ -492,8 +519,11 @@ __device__ void consume_pairs(const FusedArgs<T>& A, const SmemPlan& S, int ns, 
   }
 }
 
-template <typename T, int RP, int RQ>
-__global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A, SmemPlan S) {
+// BATCHED: CTAs are (set, unit) items of a batched launch (a separate
+// instantiation, so that the single-problem kernel keeps the per-set fields
+// in the parameter space instead of registers).
+template <typename T, int RP, int RQ, bool BATCHED>
+__global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A_in, SmemPlan S) {
   extern __shared__ __align__(16) unsigned char smem[];
   AntInfo<T>* sa = reinterpret_cast<AntInfo<T>*>(smem + S.off_ant);
   SrcInfo<T>* ss = reinterpret_cast<SrcInfo<T>*>(smem + S.off_src);
@@ -503,7 +533,9 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A,
   int* items = reinterpret_cast<int*>(smem + S.off_items);
   double* red = reinterpret_cast<double*>(smem + S.off_red);
 
-  const int unit = blockIdx.x;
+  FusedArgs<T> A = A_in;
+  int unit = blockIdx.x;
+  if constexpr (BATCHED) unit = cta_unit(A);
   const int t = unit / A.nchan, ch = unit - t * A.nchan;
   load_antennas(A, t, ch, sa);
   for (int i = threadIdx.x; i < S.npairs; i += blockDim.x) {
@@ -725,8 +757,8 @@ __device__ __forceinline__ SrcInfo<float> point_source_stokes(const FusedArgs<fl
   return si;
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float> A, SmemPlan S, TcPlan P) {
+template <int MODE, bool BATCHED>
+__global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float> A_in, SmemPlan S, TcPlan P) {
   constexpr int kRowBytes = TcGeom<MODE>::kRowBytes;
   constexpr int KAPPA = TcGeom<MODE>::kSlots;  // source slots per stage
   constexpr int NSRC = kTcProducerWarps;       // sources per stage
@@ -751,7 +783,9 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int unit = blockIdx.x;
+  FusedArgs<float> A = A_in;
+  int unit = blockIdx.x;
+  if constexpr (BATCHED) unit = cta_unit(A);
   const int t = unit / A.nchan, ch = unit - t * A.nchan;
   if (tid == 0) *abort_flag = A.err ? *reinterpret_cast<volatile int*>(A.err) : 0;
   __syncthreads();
@@ -1364,8 +1398,8 @@ __device__ void adj_flush(const FusedArgs<T>& A, int t, int s0, int ns, T* sacc)
   }
 }
 
-template <typename T, int RA, int RS>
-__global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<T> A, SmemPlan S) {
+template <typename T, int RA, int RS, bool BATCHED>
+__global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<T> A_in, SmemPlan S) {
   extern __shared__ __align__(16) unsigned char smem[];
   AntInfo<T>* sa = reinterpret_cast<AntInfo<T>*>(smem + S.off_ant);
   SrcInfo<T>* ss = reinterpret_cast<SrcInfo<T>*>(smem + S.off_src);
@@ -1374,7 +1408,9 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
   Jones<T>* sX = reinterpret_cast<Jones<T>*>(smem + S.off_V);
   T* sacc = reinterpret_cast<T*>(smem + S.off_acc);
 
-  const int unit = blockIdx.x;
+  FusedArgs<T> A = A_in;
+  int unit = blockIdx.x;
+  if constexpr (BATCHED) unit = cta_unit(A);
   const int t = unit / A.nchan, ch = unit - t * A.nchan;
   load_antennas(A, t, ch, sa);
   const int nx = AdjTile<T>::FULL_Y ? A.na * y_row_vals<T>(A.na) : 8 * S.npairs;
@@ -1439,8 +1475,8 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
 // (the second with the instruction's negate-A bit), each operand as
 // hi.hi + hi.lo + lo.hi.
 //
-// Worker warps 0-7 form two groups of four (one warp per TMEM lane quarter)
-// that take alternate tiles.  Worker lane (a, i) = TMEM lane 2a + i handles
+// The 12 worker warps form three groups of four (one warp per TMEM lane
+// quarter) that take every third tile.  Worker lane (a, i) = TMEM lane 2a + i handles
 // the items (source 4i + u, antenna a), u = 0..3, of its group's tile: it
 // computes E, dE/dl, dE/dm, K and J once, stages J for the MMA and parks
 //   EK = E K,  DL = dE/dl K,  DM = dE/dm K
@@ -1450,7 +1486,8 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
 //   d/dphi = 2 pi nu / c * Im tr(d sqrt(B)^H sqrt(B)).
 // Lane 0 of the group's first and second warps issue the Re and Im MMA
 // chains once the group has staged its tile (group barrier); while one group
-// waits for its MMAs the others compute.
+// waits for its MMAs the others compute.  Y itself is formed at the start of
+// the CTA from d chi^2 / dV (the forward's epilogue output) and stays in TMEM.
 constexpr int kTaRowBytes = 512;      // 256 BF16 values of K per operand row
 constexpr int kTaKappa = 8;           // sources per tile (16 operand rows)
 constexpr int kTaGroups = 3;          // worker groups = stages = TMEM regions
@@ -1473,50 +1510,11 @@ constexpr int kTaAcc = 6;
 static_assert(kTaAcc <= 8, "per-source sums fit the 8-value reduce-scatter");
 using TaGeom = StageGeometry<kTaRowBytes>;
 using TaLayout = StageLayout<MB_MODE_SPLIT_BF16, kTaRowBytes>;
-constexpr size_t kYopBytes = 2 * size_t(TaGeom::kMatBytes);          // hi + lo: 128 KB
 constexpr size_t kJopBytes = 2 * size_t(2 * 8 * kTaRowBytes);       // hi + lo, 16 rows
-
-// Y of one (time, channel) unit from d chi^2 / dV, written as the BF16
-// hi + lo tensor-core operand above (A_hi at +0, A_lo at +64 KB).
-__global__ void yop_build_kernel(FusedArgs<float> A) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  Jones<float>* sY = reinterpret_cast<Jones<float>*>(smem);
-  const int unit = blockIdx.x;
-  const int t = unit / A.nchan, ch = unit - t * A.nchan;
-  const int na = A.na;
-  for (int i = threadIdx.x; i < na * na; i += blockDim.x) sY[i] = jzero<float>();
-  __syncthreads();
-  for (int bl = threadIdx.x; bl < A.nbl; bl += blockDim.x) {
-    const size_t tbl = size_t(t) * A.lnbl + bl;
-    const int p = A.ant1[tbl], q = A.ant2[tbl];
-    if (p < 0 || p >= na || q < 0 || q >= na) continue;
-    const Jones<float> g = jload<float>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch));
-    atomic_add_jones(&sY[p * na + q], g);
-    atomic_add_jones(&sY[q * na + p], jherm(g));
-  }
-  __syncthreads();
-  // row r: 128 words of hi parts, then 128 words of lo parts; word kp holds
-  // K = 2kp (low half) and 2kp + 1: j = 0, 1 of antenna b
-  uint32_t* yw = reinterpret_cast<uint32_t*>(A.yop + size_t(unit) * kYopBytes);
-  for (int idx = threadIdx.x; idx < 128 * 128; idx += blockDim.x) {
-    const int r = idx >> 7, kp = idx & 127;
-    const int a = r >> 1, i = r & 1;
-    const bool im = kp >= 64;
-    const int b = im ? kp - 64 : kp;
-    float x0 = 0.f, x1 = 0.f;
-    if (a < na && b < na) {
-      const Jones<float> y = sY[a * na + b];
-      const Cx<float> y0 = i ? y.c : y.a, y1 = i ? y.d : y.b;  // Y_ab[i][0], Y_ab[i][1]
-      x0 = im ? -y0.i : y0.r;
-      x1 = im ? -y1.i : y1.r;
-    }
-    __nv_bfloat16 h0, l0, h1, l1;
-    tc::split_bf16(x0, h0, l0);
-    tc::split_bf16(x1, h1, l1);
-    yw[r * 256 + kp] = uint32_t(__bfloat16_as_ushort(h0)) | (uint32_t(__bfloat16_as_ushort(h1)) << 16);
-    yw[r * 256 + 128 + kp] = uint32_t(__bfloat16_as_ushort(l0)) | (uint32_t(__bfloat16_as_ushort(l1)) << 16);
-  }
-}
+constexpr int kTaParkBytes = int(sizeof(float4)) * kTaGroups * kTaItems * kTaPark * 128;
+// Bytes per row of Y (na Jones + 32) while it is formed in the park region.
+constexpr int kTaYRowBytes = 64 * int(sizeof(Jones<float>)) + 32;
+static_assert(64 * kTaYRowBytes <= kTaParkBytes, "Y of 64 antennas fits the park region");
 
 // Sum of v[k] over the 16 lanes that share lane bit 0, by reduce-scatter
 // over lane bits 4, 3, 2 and a plain sum over bit 1 (8 shuffles for 8
@@ -1605,7 +1603,8 @@ __device__ __forceinline__ void ta_issue_chain(bool im, uint32_t d, uint32_t ytm
   }
 }
 
-__global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<float> A, TaPlan P) {
+template <bool BATCHED>
+__global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<float> A_in, TaPlan P) {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* park = reinterpret_cast<float4*>(smem + P.off_park);  // [group][item][kTaPark][128 lanes]
   unsigned char* stage = smem + P.off_stage;  // [kTaGroups][kJopBytes]
@@ -1619,7 +1618,9 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int unit = blockIdx.x;
+  FusedArgs<float> A = A_in;
+  int unit = blockIdx.x;
+  if constexpr (BATCHED) unit = cta_unit(A);
   const int t = unit / A.nchan, ch = unit - t * A.nchan;
   if (tid == 0) *abort_flag = A.err ? *reinterpret_cast<volatile int*>(A.err) : 0;
   __syncthreads();
@@ -1640,18 +1641,52 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
   __syncthreads();
   tc::fence_after_thread_sync();
   const uint32_t tmem = *tmem_slot;
-  // Y operand of this unit into TMEM columns 0-255: row r = TMEM lane r;
-  // the three warps of a lane quarter share the row's 8 runs of 32 words.
+  // Y of this unit from d chi^2 / dV, formed in the park region (unused until
+  // the tile sweep): baseline (p, q) adds gV to Y_pq and gV^H to Y_qp (both to
+  // Y_pp for an autocorrelation; repeated pairs sum).  Rows of Y are padded
+  // by 32 bytes, so the 16-byte loads of 4 rows x 2 Jones rows that a
+  // quarter warp makes below meet distinct banks.  Then each TMEM lane r =
+  // (a, i) takes its row of the BF16 hi + lo operand: word kp of the hi half
+  // (columns 0-127) holds K = 2 kp, 2 kp + 1, i.e. Re Y_ab[i][0], Re Y_ab[i][1]
+  // for b = kp < 64 and -Im of them for b = kp - 64; the lo half (columns
+  // 128-255) likewise.  The three warps of a lane quarter share the row's 8
+  // runs of 32 words.
   {
+    unsigned char* ybase = reinterpret_cast<unsigned char*>(park);
+    const int na = A.na, yrow = kTaYRowBytes;
+    for (int x = tid; x < na * yrow / 16; x += blockDim.x)
+      reinterpret_cast<uint4*>(ybase)[x] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    for (int bl = tid; bl < A.nbl; bl += blockDim.x) {
+      const size_t tbl = size_t(t) * A.lnbl + bl;
+      const int p = A.ant1[tbl], q = A.ant2[tbl];
+      if (p < 0 || p >= na || q < 0 || q >= na) continue;
+      const Jones<float> g = jload<float>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch));
+      atomic_add_jones(reinterpret_cast<Jones<float>*>(ybase + size_t(p) * yrow) + q, g);
+      atomic_add_jones(reinterpret_cast<Jones<float>*>(ybase + size_t(q) * yrow) + p, jherm(g));
+    }
+    __syncthreads();
     const int q = warp & 3, part = warp >> 2;
-    const int r = 32 * q + lane;
-    const uint4* src = reinterpret_cast<const uint4*>(A.yop + size_t(unit) * kYopBytes) + r * 64;
+    const int r = 32 * q + lane, a = r >> 1, i = r & 1;
+    const float* yr = reinterpret_cast<const float*>(ybase + size_t(a < na ? a : 0) * yrow) + 4 * i;
     for (int run = part; run < 8; run += kTaGroups) {
+      const bool lo_half = run >= 4, im = (run & 3) >= 2;
+      const int b0 = 32 * (run & 1);
       uint32_t w[32];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const uint4 x = __ldg(src + 8 * run + k);
-        w[4 * k] = x.x; w[4 * k + 1] = x.y; w[4 * k + 2] = x.z; w[4 * k + 3] = x.w;
+      for (int k = 0; k < 32; ++k) {
+        const int b = b0 + k;
+        float x0 = 0.f, x1 = 0.f;
+        if (a < na && b < na) {
+          const float4 y4 = *reinterpret_cast<const float4*>(yr + 8 * b);  // Y_ab[i][0], Y_ab[i][1]
+          x0 = im ? -y4.y : y4.x;
+          x1 = im ? -y4.w : y4.z;
+        }
+        __nv_bfloat16 h0, l0, h1, l1;
+        tc::split_bf16(x0, h0, l0);
+        tc::split_bf16(x1, h1, l1);
+        w[k] = lo_half ? (uint32_t(__bfloat16_as_ushort(l0)) | (uint32_t(__bfloat16_as_ushort(l1)) << 16))
+                       : (uint32_t(__bfloat16_as_ushort(h0)) | (uint32_t(__bfloat16_as_ushort(h1)) << 16));
       }
       tc::tmem_st32(tmem + (uint32_t(32 * q) << 16) + uint32_t(32 * run), w);
     }
@@ -1940,7 +1975,12 @@ __global__ void beam_plane_kernel(FusedArgs<T> A, T* __restrict__ plane) {
 // [s][t][8] = ((I+Q+s0)/tau, (I-Q+s0)/tau, U/tau, V/tau, alpha/2, 0, 0, 0):
 // 32-byte entries, so the first four values are one aligned 16-byte load.
 template <typename T>
-__global__ void bsqrt_ref_kernel(FusedArgs<T> A, T* __restrict__ tab) {
+__global__ void bsqrt_ref_kernel(FusedArgs<T> A_in, T* __restrict__ tab) {
+  FusedArgs<T> A = A_in;
+  if (A.bsets) {  // batched: grid.y = set, the set's own table
+    use_set(A, A.bsets[blockIdx.y]);
+    tab = const_cast<T*>(A.bsq0);
+  }
   const size_t total = size_t(A.nsrc) * A.ntime;
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
     const int s = int(i / A.ntime), t = int(i % A.ntime);
@@ -1959,7 +1999,12 @@ __global__ void bsqrt_ref_kernel(FusedArgs<T> A, T* __restrict__ tab) {
 }
 
 template <typename T>
-__global__ void phi_kernel(FusedArgs<T> A, double* __restrict__ phi) {
+__global__ void phi_kernel(FusedArgs<T> A_in, double* __restrict__ phi) {
+  FusedArgs<T> A = A_in;
+  if (A.bsets) {  // batched: grid.y = set, the set's own table
+    use_set(A, A.bsets[blockIdx.y]);
+    phi = const_cast<double*>(A.phi);
+  }
   size_t total = size_t(A.ntime) * A.nsrc * A.na;
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
     int a = int(i % A.na);
@@ -1973,9 +2018,16 @@ __global__ void phi_kernel(FusedArgs<T> A, double* __restrict__ phi) {
 }
 
 template <typename T>
-__global__ void finalize_grads_kernel(FusedArgs<T> A, double scale, T* __restrict__ g_lm, T* __restrict__ g_stokes,
+__global__ void finalize_grads_kernel(FusedArgs<T> A_in, double scale, T* __restrict__ g_lm, T* __restrict__ g_stokes,
                                       T* __restrict__ g_alpha, T* __restrict__ g_gauss, T* __restrict__ g_sersic,
                                       T* __restrict__ g_G) {
+  FusedArgs<T> A = A_in;
+  if (A.bsets) {  // batched: grid.y = set, the set's accumulators and outputs
+    const BatchSet<T>& b = A.bsets[blockIdx.y];
+    use_set(A, b);
+    g_lm = b.g_lm; g_stokes = b.g_stokes; g_alpha = b.g_alpha;
+    g_gauss = b.g_gauss; g_sersic = b.g_sersic; g_G = b.g_G;
+  }
   const size_t n_lm = size_t(A.nsrc) * 2, n_st = size_t(A.nsrc) * A.ntime;
   const size_t n_g = size_t(3) * A.ngsrc, n_x = size_t(3) * A.nssrc;
   const size_t n_G = size_t(A.ntime) * A.na * A.nchan;
@@ -2006,12 +2058,30 @@ __global__ void finalize_grads_kernel(FusedArgs<T> A, double scale, T* __restric
   }
 }
 
+// chi^2 of every set of a batch: block b sums set b's unit partials in a
+// fixed order (deterministic), X2[b] = scale * sum.
+template <typename T>
+__global__ void sum_partials_sets_kernel(const BatchSet<T>* __restrict__ sets, int units, double scale,
+                                         double* __restrict__ X2) {
+  __shared__ double red[32];
+  const double* partial = sets[blockIdx.x].partial;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < units; i += blockDim.x) acc += partial[i];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) X2[blockIdx.x] = acc * scale;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 struct WsLayout {
-  size_t phi, plane, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, err, yop,
-      total;
+  size_t phi, plane, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, err, total;
 };
 
 WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_grad) {
@@ -2034,7 +2104,6 @@ WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_gra
   L.acc_sersic = take(want_grad ? 3 * nx * 8 : 0);
   L.acc_end = o;
   L.err = take(sizeof(int));
-  L.yop = take(want_grad && mode != MB_MODE_NATIVE && dtype == MB_FLOAT32 ? nt * nc * kYopBytes : 0);
   L.total = o;
   return L;
 }
@@ -2048,7 +2117,8 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.ltime = d->ntime.local_size; A.lna = d->na.local_size; A.lnbl = d->nbl.local_size;
   A.lchan = d->nchan.local_size; A.lgsrc = d->ngsrc.local_size; A.lssrc = d->nssrc.local_size;
   A.lw = d->beam_lw.local_size; A.mh = d->beam_mh.local_size; A.nud = d->beam_nud.local_size;
-  A.t0 = 0; A.ch0 = 0; A.sbeg = 0;
+  A.sbeg = 0;
+  A.bsets = nullptr; A.bitems = nullptr;
   A.accumulate_in = d->nsrc.lower_extent > 0;
   A.partial_out = d->nsrc.upper_extent < d->nsrc.global_size;
   A.weights = options & MB_APPLY_WEIGHTS;
@@ -2071,7 +2141,7 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.model_vis = (T*)model_vis; A.chi2 = (T*)chi2;
   A.err = nullptr;
   A.phi = nullptr; A.partial = nullptr; A.gV = nullptr; A.dG = nullptr;
-  A.plane = nullptr; A.bsq0 = nullptr; A.yop = nullptr;
+  A.plane = nullptr; A.bsq0 = nullptr;
   A.acc_lm = A.acc_stokes = A.acc_alpha = A.acc_gauss = A.acc_sersic = nullptr;
   if (ws == nullptr) return MB_OK;
   char* w = static_cast<char*>(ws);
@@ -2087,7 +2157,6 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.acc_gauss = reinterpret_cast<double*>(w + L.acc_gauss);
   A.acc_sersic = reinterpret_cast<double*>(w + L.acc_sersic);
   A.err = reinterpret_cast<int*>(w + L.err);
-  A.yop = (want_grad && L.yop != L.total) ? reinterpret_cast<unsigned char*>(w + L.yop) : nullptr;
   return MB_OK;
 }
 
@@ -2153,10 +2222,14 @@ mb_status launch_prep(const FusedArgs<T>& A, void* ws, const WsLayout& L, cudaSt
   return MB_OK;
 }
 
-mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2, cudaStream_t stream) {
+// Kernel launchers over `grid` CTAs: a single problem's (time, channel)
+// units, or a batched launch's (set, unit) items (A.bitems).
+
+// Split-precision forward: point sources on the tensor cores, extended
+// sources on the CUDA cores in the same CTA.
+mb_status run_tc_fwd(const FusedArgs<float>& A, mb_mode mode, int grid, cudaStream_t stream) {
   if (A.na > 64)
     return fail(MB_ERR_UNSUPPORTED, "split-precision modes handle up to 64 antennas (got %d)", A.na);
-  const int units = A.ntime * A.nchan;
   // The stage region holds the operand stages during the tensor-core phase,
   // then the extended sources' Jones tile and the FP32 low parts of the pair
   // accumulators.  All regions 128-byte aligned.  The extended sources take
@@ -2195,21 +2268,70 @@ mb_status launch_tc_forward(const FusedArgs<float>& A, mb_mode mode, double* X2,
   if (P.total > kMaxDynamicSmem)
     return fail(MB_ERR_UNSUPPORTED, "split-precision kernel needs %zu bytes of shared memory for na=%d",
                 P.total, A.na);
+  if (grid == 0) return MB_OK;
   if (mode == MB_MODE_SPLIT_TF32) {
-    auto kern = coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32>;
+    auto kern = A.bitems ? coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32, true> : coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32, false>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
-    { KernelScope ks_("coh_tc_fwd_kernel", stream); kern<<<units, kTcThreads, P.total, stream>>>(A, S, P); }
+    { KernelScope ks_("coh_tc_fwd_kernel", stream); kern<<<grid, kTcThreads, P.total, stream>>>(A, S, P); }
   } else {
-    auto kern = coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16>;
+    auto kern = A.bitems ? coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16, true> : coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16, false>;
     MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
-    { KernelScope ks_("coh_tc_fwd_kernel", stream); kern<<<units, kTcThreads, P.total, stream>>>(A, S, P); }
+    { KernelScope ks_("coh_tc_fwd_kernel", stream); kern<<<grid, kTcThreads, P.total, stream>>>(A, S, P); }
   }
-  MB_CHECK(check_launch("coh_tc_fwd_kernel"));
-  {
-    KernelScope ks_("sum_partials_kernel", stream);
-    sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, A.weights ? 1.0 : A.inv_sigma2, X2);
-  }
-  return check_launch("sum_partials_kernel");
+  return check_launch("coh_tc_fwd_kernel");
+}
+
+// CUDA-core forward (FP64, plain FP32).
+template <typename T>
+mb_status run_fwd(const FusedArgs<T>& A, int grid, cudaStream_t stream) {
+  constexpr int RP = FwdTile<T>::RP, RQ = FwdTile<T>::RQ;
+  SmemPlan S = make_plan<T>(A.na, false, true, A.src_tile);
+  if (S.total > kMaxDynamicSmem)
+    return fail(MB_ERR_UNSUPPORTED, "fused forward needs %zu bytes of shared memory for na=%d (max 232448)",
+                S.total, A.na);
+  if (grid == 0) return MB_OK;
+  auto kern = A.bitems ? coh_fwd_kernel<T, RP, RQ, true> : coh_fwd_kernel<T, RP, RQ, false>;
+  MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
+  { KernelScope ks_("coh_fwd_kernel", stream); kern<<<grid, S.nthreads, S.total, stream>>>(A, S); }
+  return check_launch("coh_fwd_kernel");
+}
+
+// Split-precision adjoint of the point sources: dJ = Y J on the tensor cores.
+mb_status run_tc_adj(const FusedArgs<float>& A, int grid, cudaStream_t stream) {
+  if (A.na > 64)
+    return fail(MB_ERR_UNSUPPORTED, "split-precision modes handle up to 64 antennas (got %d)", A.na);
+  if (grid == 0) return MB_OK;
+  TaPlan P;
+  size_t o = 0;
+  auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 128); return r; };
+  P.off_park = take(kTaParkBytes);
+  P.off_stage = take(size_t(kTaGroups) * kJopBytes);
+  P.off_ant = take(sizeof(AntInfo<float>) * A.na);
+  P.off_acc = take(sizeof(float) * kTaGroups * 2 * kTaKappa * kTaAcc);
+  P.off_src = take(sizeof(TaSrc) * kTaGroups * 2 * kTaKappa);
+  P.off_bar = take(2 * kTaGroups * sizeof(uint64_t) + 16);
+  P.total = o;
+  auto kern = A.bitems ? coh_tc_adj_kernel<true> : coh_tc_adj_kernel<false>;
+  MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
+  { KernelScope ks_("coh_tc_adj_kernel", stream); kern<<<grid, kTaThreads, P.total, stream>>>(A, P); }
+  return check_launch("coh_tc_adj_kernel");
+}
+
+// CUDA-core adjoint: all sources from A.sbeg (FP64, plain FP32), or only the
+// extended sources of a split-precision call (ext_only: no dchi^2/dJ tile,
+// 32-source tiles by default).
+template <typename T>
+mb_status run_adj(const FusedArgs<T>& A, bool ext_only, int grid, cudaStream_t stream) {
+  constexpr int RA = AdjTile<T>::RA, RS = AdjTile<T>::RS;
+  SmemPlan S = ext_only ? make_plan<T>(A.na, true, true, A.src_tile ? A.src_tile : 32, false)
+                        : make_plan<T>(A.na, true, true, A.src_tile);
+  if (S.total > kMaxDynamicSmem)
+    return fail(MB_ERR_UNSUPPORTED, "fused adjoint needs %zu bytes of shared memory for na=%d", S.total, A.na);
+  if (grid == 0) return MB_OK;
+  auto kern = A.bitems ? coh_adj_kernel<T, RA, RS, true> : coh_adj_kernel<T, RA, RS, false>;
+  MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
+  { KernelScope ks_("coh_adj_kernel", stream); kern<<<grid, S.nthreads, S.total, stream>>>(A, S); }
+  return check_launch("coh_adj_kernel");
 }
 
 template <typename T>
@@ -2222,66 +2344,33 @@ mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* 
     return MB_OK;
   }
   MB_CHECK(launch_prep(A, ws, L, stream));
+  bool done = false;
   if constexpr (sizeof(T) == 4) {
-    if (mode != MB_MODE_NATIVE) return launch_tc_forward(A, mode, X2, stream);
+    if (mode != MB_MODE_NATIVE) {
+      MB_CHECK(run_tc_fwd(A, mode, units, stream));
+      done = true;
+    }
   }
-  const FusedArgs<T>& B = A;
-  constexpr int RP = FwdTile<T>::RP, RQ = FwdTile<T>::RQ;
-  SmemPlan S = make_plan<T>(A.na, false, true, A.src_tile);
-  if (S.total > kMaxDynamicSmem)
-    return fail(MB_ERR_UNSUPPORTED, "fused forward needs %zu bytes of shared memory for na=%d (max 232448)",
-                S.total, A.na);
-  auto kern = coh_fwd_kernel<T, RP, RQ>;
-  MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
-  { KernelScope ks_("coh_fwd_kernel", stream); kern<<<units, S.nthreads, S.total, stream>>>(B, S); }
-  MB_CHECK(check_launch("coh_fwd_kernel"));
-  const double scale = A.weights ? 1.0 : A.inv_sigma2;
+  if (!done) MB_CHECK(run_fwd(A, units, stream));
   {
     KernelScope ks_("sum_partials_kernel", stream);
-    sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, scale, X2);
+    sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, A.weights ? 1.0 : A.inv_sigma2, X2);
   }
   return check_launch("sum_partials_kernel");
 }
 
-// Split-precision adjoint: Y operands, point sources on the tensor cores,
-// extended sources on the CUDA cores (same FP64 accumulators).
+// Split-precision adjoint: point sources on the tensor cores, extended
+// sources on the CUDA cores (same FP64 accumulators).
 mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
   if (A.na > 64)
     return fail(MB_ERR_UNSUPPORTED, "split-precision modes handle up to 64 antennas (got %d)", A.na);
-  if (A.yop == nullptr) return fail(MB_ERR_WORKSPACE, "workspace lacks the adjoint operand region");
   const int units = A.ntime * A.nchan;
   // the error word is the forward's (cleared there): an adjoint after a
   // forward whose waits gave up does no work and keeps reporting it
-  if (A.npsrc > 0) {
-    const size_t ysmem = size_t(A.na) * A.na * sizeof(Jones<float>);
-    MB_CUDA(cudaFuncSetAttribute(yop_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(ysmem)));
-    { KernelScope ks_("yop_build_kernel", stream); yop_build_kernel<<<units, 256, ysmem, stream>>>(A); }
-    MB_CHECK(check_launch("yop_build_kernel"));
-    TaPlan P;
-    size_t o = 0;
-    auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 128); return r; };
-    P.off_park = take(sizeof(float4) * kTaGroups * kTaItems * kTaPark * 128);
-    P.off_stage = take(size_t(kTaGroups) * kJopBytes);
-    P.off_ant = take(sizeof(AntInfo<float>) * A.na);
-    P.off_acc = take(sizeof(float) * kTaGroups * 2 * kTaKappa * kTaAcc);
-    P.off_src = take(sizeof(TaSrc) * kTaGroups * 2 * kTaKappa);
-    P.off_bar = take(2 * kTaGroups * sizeof(uint64_t) + 16);
-    P.total = o;
-    MB_CUDA(cudaFuncSetAttribute(coh_tc_adj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
-    {
-      KernelScope ks_("coh_tc_adj_kernel", stream);
-      coh_tc_adj_kernel<<<units, kTaThreads, P.total, stream>>>(A, P);
-    }
-    MB_CHECK(check_launch("coh_tc_adj_kernel"));
-  }
+  if (A.npsrc > 0) MB_CHECK(run_tc_adj(A, units, stream));
   if (A.nsrc > A.npsrc) {
     A.sbeg = A.npsrc;
-    // extended sources only: no dchi^2/dJ tile, 32-source tiles by default
-    SmemPlan S = make_plan<float>(A.na, true, true, A.src_tile ? A.src_tile : 32, false);
-    auto kern = coh_adj_kernel<float, AdjTile<float>::RA, AdjTile<float>::RS>;
-    MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
-    { KernelScope ks_("coh_adj_kernel", stream); kern<<<units, S.nthreads, S.total, stream>>>(A, S); }
-    MB_CHECK(check_launch("coh_adj_kernel"));
+    MB_CHECK(run_adj(A, true, units, stream));
   }
   return MB_OK;
 }
@@ -2299,16 +2388,7 @@ mb_status launch_adjoint(const FusedArgs<T>& A, mb_mode mode, double grad_scale,
       done_sources = true;
     }
   }
-  if (units > 0 && A.nsrc > 0 && !done_sources) {
-    constexpr int RA = AdjTile<T>::RA, RS = AdjTile<T>::RS;
-    SmemPlan S = make_plan<T>(A.na, true, true, A.src_tile);
-    if (S.total > kMaxDynamicSmem)
-      return fail(MB_ERR_UNSUPPORTED, "fused adjoint needs %zu bytes of shared memory for na=%d", S.total, A.na);
-    auto kern = coh_adj_kernel<T, RA, RS>;
-    MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
-    { KernelScope ks_("coh_adj_kernel", stream); kern<<<units, S.nthreads, S.total, stream>>>(A, S); }
-    MB_CHECK(check_launch("coh_adj_kernel"));
-  }
+  if (units > 0 && A.nsrc > 0 && !done_sources) MB_CHECK(run_adj(A, false, units, stream));
   size_t total = size_t(A.nsrc) * 2 + size_t(A.nsrc) * A.ntime + 3 * size_t(A.ngsrc) + 3 * size_t(A.nssrc) +
                  size_t(A.ntime) * A.na * A.nchan;
   if (total > 0) {
@@ -2318,6 +2398,284 @@ mb_status launch_adjoint(const FusedArgs<T>& A, mb_mode mode, double grad_scale,
       finalize_grads_kernel<T><<<blocks, 256, 0, stream>>>(A, grad_scale, (T*)g->lm, (T*)g->stokes, (T*)g->alpha,
                                                            (T*)g->gauss_shape, (T*)g->sersic_shape, (T*)g->G_term);
     }
+    MB_CHECK(check_launch("finalize_grads_kernel"));
+  }
+  return MB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched likelihood (mb_rime_batch)
+// ---------------------------------------------------------------------------
+// Workspace: the beam plane and error word shared by all sets, the device
+// table of BatchSet entries, the (set, unit) item lists of the launches, all
+// sets' FP64 gradient accumulators (one contiguous region, cleared by one
+// memset), then per set its path-length table, sqrt(B) table (FP32), unit
+// partials, d chi^2 / dV and d chi^2 / dG.
+enum BatchKind { kBatchFwd, kBatchTcFwd, kBatchAdj, kBatchTcAdj, kBatchExtAdj };
+
+struct BatchGroup {
+  int kind, mode, tile;
+  size_t first;  // first item of the group in the item list
+  int count;     // items (CTAs)
+};
+
+struct SetOffsets {
+  size_t phi, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic;
+};
+
+struct BatchPlan {
+  size_t plane = 0, err = 0, sets = 0, items = 0, acc_begin = 0, acc_end = 0, total = 0;
+  size_t max_phi = 0, max_bsq = 0, max_grad = 0;  // largest per-set sizes of the set-grid kernels
+  std::vector<SetOffsets> off;
+  std::vector<int> order;  // sets by decreasing source count, so the longest CTAs start first
+  std::vector<BatchGroup> groups;
+  size_t nitems = 0;
+};
+
+int tile_of_options(uint32_t o) {
+  return (o & MB_SOURCE_TILE_MASK) ? 4 << ((o & MB_SOURCE_TILE_MASK) >> MB_SOURCE_TILE_SHIFT) : 0;
+}
+
+mb_status batch_plan(mb_dtype dtype, const mb_dims* d, const mb_batch_set* sets, int nsets, BatchPlan& B) {
+  if (dtype != MB_FLOAT32 && dtype != MB_FLOAT64) return fail(MB_ERR_UNSUPPORTED_DTYPE, "dtype %d", int(dtype));
+  if (nsets < 0) return fail(MB_ERR_INVALID_ARG, "nsets < 0");
+  if (nsets > 0) MB_REQUIRE(sets, "sets");
+  if (nsets > 65535) return fail(MB_ERR_UNSUPPORTED, "at most 65535 sets per batch (got %d)", nsets);
+  const size_t es = dtype == MB_FLOAT64 ? 8 : 4;
+  const size_t nt = ext(d->ntime), na = ext(d->na), nbl = ext(d->nbl), nc = ext(d->nchan);
+  const size_t units = nt * nc;
+  for (int i = 0; i < nsets; ++i) {
+    const mb_batch_set& s = sets[i];
+    const uint64_t n = uint64_t(s.npsrc) + s.ngsrc + s.nssrc;
+    if (n > 0x7fffffffu) return fail(MB_ERR_INVALID_ARG, "set %d: too many sources", i);
+    if (s.mode != MB_MODE_NATIVE && s.mode != MB_MODE_SPLIT_TF32 && s.mode != MB_MODE_SPLIT_BF16)
+      return fail(MB_ERR_INVALID_ARG, "set %d: mode %u", i, s.mode);
+    if (s.mode != MB_MODE_NATIVE && dtype != MB_FLOAT32)
+      return fail(MB_ERR_UNSUPPORTED, "set %d: split-precision modes take FLOAT32 data", i);
+    if (s.mode != MB_MODE_NATIVE && na > 64)
+      return fail(MB_ERR_UNSUPPORTED, "set %d: split-precision modes handle up to 64 antennas (got %zu)", i, na);
+    if (s.options & ~MB_SOURCE_TILE_MASK)
+      return fail(MB_ERR_INVALID_ARG, "set %d: options may only hold source-tile bits (0x%x)", i, s.options);
+    if (s.reserved != 0) return fail(MB_ERR_INVALID_ARG, "set %d: reserved must be 0", i);
+    if (n > 0) {
+      MB_REQUIRE(s.lm, "set lm"); MB_REQUIRE(s.stokes, "set stokes"); MB_REQUIRE(s.alpha, "set alpha");
+    }
+    if (s.ngsrc > 0) MB_REQUIRE(s.gauss_shape, "set gauss_shape");
+    if (s.nssrc > 0) MB_REQUIRE(s.sersic_shape, "set sersic_shape");
+  }
+  if (units * size_t(nsets) > size_t(0x7fffffff))
+    return fail(MB_ERR_UNSUPPORTED, "a batch of %d sets x %zu units exceeds 2^31 CTAs", nsets, units);
+  size_t o = 0;
+  auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 256); return r; };
+  B.plane = take(nc * size_t(d->beam_lw.local_size) * d->beam_mh.local_size * kPlaneVals * es);
+  B.err = take(sizeof(int));
+  B.sets = take(size_t(nsets) * sizeof(BatchSet<float>));
+  B.order.resize(nsets);
+  for (int i = 0; i < nsets; ++i) B.order[i] = i;
+  auto nsrc_of = [&](int i) { return uint64_t(sets[i].npsrc) + sets[i].ngsrc + sets[i].nssrc; };
+  std::stable_sort(B.order.begin(), B.order.end(), [&](int a, int b) { return nsrc_of(a) > nsrc_of(b); });
+  // launch groups: forward groups, then adjoint groups, each in first-seen order
+  B.groups.clear();
+  auto group_of = [&](int kind, int mode, int tile) -> BatchGroup& {
+    for (auto& g : B.groups)
+      if (g.kind == kind && g.mode == mode && g.tile == tile) return g;
+    B.groups.push_back(BatchGroup{kind, mode, tile, 0, 0});
+    return B.groups.back();
+  };
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i : B.order) {
+      const mb_batch_set& s = sets[i];
+      const int tile = tile_of_options(s.options);
+      const bool tc = s.mode != MB_MODE_NATIVE;
+      if (pass == 0) {
+        group_of(tc ? kBatchTcFwd : kBatchFwd, tc ? int(s.mode) : 0, tile).count += int(units);
+      } else {
+        if (tc && s.npsrc > 0) group_of(kBatchTcAdj, 0, 0).count += int(units);
+        if (tc && s.ngsrc + s.nssrc > 0) group_of(kBatchExtAdj, 0, tile).count += int(units);
+        if (!tc && nsrc_of(i) > 0) group_of(kBatchAdj, 0, tile).count += int(units);
+      }
+    }
+  }
+  B.nitems = 0;
+  for (auto& g : B.groups) {
+    g.first = B.nitems;
+    B.nitems += size_t(g.count);
+  }
+  B.items = take(B.nitems * sizeof(int2));
+  B.off.assign(nsets, SetOffsets{});
+  B.acc_begin = o;
+  for (int i = 0; i < nsets; ++i) {
+    const size_t ns = nsrc_of(i);
+    SetOffsets& so = B.off[i];
+    so.acc_lm = take(ns * 2 * 8);
+    so.acc_stokes = take(ns * nt * 4 * 8);
+    so.acc_alpha = take(ns * nt * 8);
+    so.acc_gauss = take(3 * size_t(sets[i].ngsrc) * 8);
+    so.acc_sersic = take(3 * size_t(sets[i].nssrc) * 8);
+  }
+  B.acc_end = o;
+  B.max_phi = B.max_bsq = B.max_grad = 0;
+  for (int i = 0; i < nsets; ++i) {
+    const size_t ns = nsrc_of(i);
+    SetOffsets& so = B.off[i];
+    so.phi = take(nt * ns * na * 8);
+    so.bsq0 = take(dtype == MB_FLOAT32 ? ns * nt * kBsqVals * es : 0);
+    so.partial = take(units * 8);
+    so.gV = take(nt * nbl * nc * 8 * es);
+    so.dG = take(nt * na * nc * 8 * es);
+    B.max_phi = std::max(B.max_phi, nt * ns * na);
+    B.max_bsq = std::max(B.max_bsq, ns * nt);
+    B.max_grad = std::max(B.max_grad, ns * 2 + ns * nt + 3 * size_t(sets[i].ngsrc) + 3 * size_t(sets[i].nssrc) +
+                                          nt * na * nc);
+  }
+  B.total = o;
+  return MB_OK;
+}
+
+// The observation's dims with the sources taken out (the sets bring theirs).
+mb_dims batch_obs_dims(const mb_dims* d) {
+  mb_dims o = *d;
+  const mb_dim none = {0, 0, 0, 0};
+  o.nsrc = o.npsrc = o.ngsrc = o.nssrc = none;
+  return o;
+}
+
+template <typename T>
+mb_status batch_prepare(const mb_dims* d, const mb_batch_set* sets, int nsets, void* ws, const BatchPlan& B,
+                        cudaStream_t stream) {
+  char* w = static_cast<char*>(ws);
+  const int units = int(ext(d->ntime) * ext(d->nchan));
+  std::vector<BatchSet<T>> bs(nsets);
+  for (int i = 0; i < nsets; ++i) {
+    const mb_batch_set& s = sets[i];
+    const SetOffsets& so = B.off[i];
+    BatchSet<T>& b = bs[i];
+    b.lm = static_cast<const T*>(s.lm); b.stokes = static_cast<const T*>(s.stokes);
+    b.alpha = static_cast<const T*>(s.alpha); b.gauss = static_cast<const T*>(s.gauss_shape);
+    b.sersic = static_cast<const T*>(s.sersic_shape);
+    b.phi = reinterpret_cast<const double*>(w + so.phi);
+    b.bsq0 = sizeof(T) == 4 ? reinterpret_cast<const T*>(w + so.bsq0) : nullptr;
+    b.partial = reinterpret_cast<double*>(w + so.partial);
+    b.gV = reinterpret_cast<T*>(w + so.gV);
+    b.dG = reinterpret_cast<T*>(w + so.dG);
+    b.acc_lm = reinterpret_cast<double*>(w + so.acc_lm);
+    b.acc_stokes = reinterpret_cast<double*>(w + so.acc_stokes);
+    b.acc_alpha = reinterpret_cast<double*>(w + so.acc_alpha);
+    b.acc_gauss = reinterpret_cast<double*>(w + so.acc_gauss);
+    b.acc_sersic = reinterpret_cast<double*>(w + so.acc_sersic);
+    b.g_lm = static_cast<T*>(s.grads.lm); b.g_stokes = static_cast<T*>(s.grads.stokes);
+    b.g_alpha = static_cast<T*>(s.grads.alpha); b.g_gauss = static_cast<T*>(s.grads.gauss_shape);
+    b.g_sersic = static_cast<T*>(s.grads.sersic_shape); b.g_G = static_cast<T*>(s.grads.G_term);
+    b.npsrc = int(s.npsrc); b.ngsrc = int(s.ngsrc); b.nssrc = int(s.nssrc); b.pad = 0;
+  }
+  std::vector<int2> items(B.nitems);
+  for (const BatchGroup& g : B.groups) {
+    size_t k = g.first;
+    for (int i : B.order) {
+      const mb_batch_set& s = sets[i];
+      const bool tc = s.mode != MB_MODE_NATIVE;
+      const int tile = tile_of_options(s.options);
+      const uint64_t n = uint64_t(s.npsrc) + s.ngsrc + s.nssrc;
+      bool in = false;
+      switch (g.kind) {
+        case kBatchFwd: in = !tc && g.tile == tile; break;
+        case kBatchTcFwd: in = tc && g.mode == int(s.mode) && g.tile == tile; break;
+        case kBatchTcAdj: in = tc && s.npsrc > 0; break;
+        case kBatchExtAdj: in = tc && s.ngsrc + s.nssrc > 0 && g.tile == tile; break;
+        case kBatchAdj: in = !tc && n > 0 && g.tile == tile; break;
+      }
+      if (!in) continue;
+      for (int u = 0; u < units; ++u) items[k++] = make_int2(i, u);
+    }
+    if (k != g.first + size_t(g.count)) return fail(MB_ERR_INVALID_ARG, "batch plan: item count mismatch");
+  }
+  if (nsets > 0)
+    MB_CUDA(cudaMemcpyAsync(w + B.sets, bs.data(), sizeof(BatchSet<T>) * nsets, cudaMemcpyHostToDevice, stream));
+  if (!items.empty())
+    MB_CUDA(cudaMemcpyAsync(w + B.items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice, stream));
+  MB_CUDA(cudaStreamSynchronize(stream));
+  return MB_OK;
+}
+
+template <typename T>
+mb_status batch_run(const mb_dims* d, const mb_props* P, uint32_t options, const mb_rime_inputs* in, int nsets,
+                    double* X2, double grad_scale, void* ws, const BatchPlan& B, cudaStream_t stream) {
+  char* w = static_cast<char*>(ws);
+  const mb_dims od = batch_obs_dims(d);
+  WsLayout unused{};
+  FusedArgs<T> A;
+  fill_args(A, &od, P, options, in, nullptr, nullptr, true, nullptr, unused);
+  A.plane = reinterpret_cast<const T*>(w + B.plane);
+  A.err = reinterpret_cast<int*>(w + B.err);
+  A.bsets = reinterpret_cast<const BatchSet<T>*>(w + B.sets);
+  const int2* items = reinterpret_cast<const int2*>(w + B.items);
+  const int units = A.ntime * A.nchan;
+  MB_CUDA(cudaMemsetAsync(A.err, 0, sizeof(int), stream));
+  if (B.acc_end > B.acc_begin) MB_CUDA(cudaMemsetAsync(w + B.acc_begin, 0, B.acc_end - B.acc_begin, stream));
+  if (nsets == 0) return MB_OK;
+  auto blocks_for = [](size_t n) { return unsigned(std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 4096))); };
+  // shared beam plane, then the per-set tables (grid.y = set)
+  size_t n = size_t(A.nchan) * A.lw * A.mh;
+  if (n > 0) {
+    { KernelScope ks_("beam_plane_kernel", stream);
+      beam_plane_kernel<T><<<blocks_for(n), 256, 0, stream>>>(A, const_cast<T*>(A.plane)); }
+    MB_CHECK(check_launch("beam_plane_kernel"));
+  }
+  if (B.max_phi > 0) {
+    { KernelScope ks_("phi_kernel", stream);
+      phi_kernel<T><<<dim3(blocks_for(B.max_phi), nsets), 256, 0, stream>>>(A, nullptr); }
+    MB_CHECK(check_launch("phi_kernel"));
+  }
+  if (sizeof(T) == 4 && B.max_bsq > 0) {
+    { KernelScope ks_("bsqrt_ref_kernel", stream);
+      bsqrt_ref_kernel<T><<<dim3(blocks_for(B.max_bsq), nsets), 256, 0, stream>>>(A, nullptr); }
+    MB_CHECK(check_launch("bsqrt_ref_kernel"));
+  }
+  // forward: one launch per (form, source tile) over all its sets' units
+  for (const BatchGroup& g : B.groups) {
+    if (g.kind != kBatchFwd && g.kind != kBatchTcFwd) continue;
+    FusedArgs<T> Ag = A;
+    Ag.src_tile = g.tile;
+    Ag.bitems = items + g.first;
+    if constexpr (sizeof(T) == 4) {
+      if (g.kind == kBatchTcFwd) {
+        MB_CHECK(run_tc_fwd(Ag, mb_mode(g.mode), g.count, stream));
+        continue;
+      }
+    }
+    if (g.kind == kBatchFwd) MB_CHECK(run_fwd(Ag, g.count, stream));
+  }
+  if (units > 0) {
+    { KernelScope ks_("sum_partials_kernel", stream);
+      sum_partials_sets_kernel<T><<<nsets, 256, 0, stream>>>(A.bsets, units, A.weights ? 1.0 : A.inv_sigma2, X2); }
+    MB_CHECK(check_launch("sum_partials_sets_kernel"));
+  } else {
+    MB_CUDA(cudaMemsetAsync(X2, 0, sizeof(double) * nsets, stream));
+  }
+  // adjoint: point sources on the tensor cores, extended sources of those
+  // sets, CUDA-core sets
+  for (const BatchGroup& g : B.groups) {
+    if (g.kind == kBatchFwd || g.kind == kBatchTcFwd) continue;
+    FusedArgs<T> Ag = A;
+    Ag.src_tile = g.tile;
+    Ag.bitems = items + g.first;
+    if constexpr (sizeof(T) == 4) {
+      if (g.kind == kBatchTcAdj) {
+        MB_CHECK(run_tc_adj(Ag, g.count, stream));
+        continue;
+      }
+    }
+    if (g.kind == kBatchExtAdj) {
+      Ag.sbeg = -1;  // each set's extended sources
+      MB_CHECK(run_adj(Ag, true, g.count, stream));
+    } else if (g.kind == kBatchAdj) {
+      MB_CHECK(run_adj(Ag, false, g.count, stream));
+    }
+  }
+  if (B.max_grad > 0) {
+    { KernelScope ks_("finalize_grads_kernel", stream);
+      finalize_grads_kernel<T><<<dim3(blocks_for(B.max_grad), nsets), 256, 0, stream>>>(
+          A, grad_scale, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr); }
     MB_CHECK(check_launch("finalize_grads_kernel"));
   }
   return MB_OK;
@@ -2390,7 +2748,7 @@ mb_status launch_forward_noalloc(FusedArgs<T> A, double* partials, double* X2, c
   if (S.total > kMaxDynamicSmem)
     return fail(MB_ERR_UNSUPPORTED, "fused forward needs %zu bytes of shared memory for na=%d (max 232448)",
                 S.total, A.na);
-  auto kern = coh_fwd_kernel<T, RP, RQ>;
+  auto kern = coh_fwd_kernel<T, RP, RQ, false>;
   MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
   { KernelScope ks_("coh_fwd_kernel", stream); kern<<<units, S.nthreads, S.total, stream>>>(A, S); }
   MB_CHECK(check_launch("coh_fwd_kernel"));
@@ -2522,6 +2880,55 @@ mb_status mb_rime_forward_noalloc(mb_dtype dtype, const mb_dims* dims, const mb_
   FusedArgs<double> A;
   fill_args(A, dims, props, options, in, model_vis, chi_sqrd_result, false, nullptr, L);
   return launch_forward_noalloc(A, partials, X2, s);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+size_t mb_rime_batch_workspace_size(mb_dtype dtype, const mb_dims* dims, const mb_batch_set* sets, int nsets) {
+  if (check_dims(dims, true) != MB_OK) return 0;
+  BatchPlan B;
+  if (batch_plan(dtype, dims, sets, nsets, B) != MB_OK) return 0;
+  return B.total;
+}
+
+mb_status mb_rime_batch_prepare(mb_dtype dtype, const mb_dims* dims, const mb_batch_set* sets, int nsets,
+                                void* workspace, size_t workspace_bytes, void* stream) {
+  MB_CHECK(check_dims(dims, true));
+  BatchPlan B;
+  MB_CHECK(batch_plan(dtype, dims, sets, nsets, B));
+  if (workspace == nullptr || workspace_bytes < B.total || (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return fail(MB_ERR_WORKSPACE, "workspace must be >= %zu bytes and 256-byte aligned (got %zu)", B.total,
+                workspace_bytes);
+  cudaStream_t s = as_stream(stream);
+  if (dtype == MB_FLOAT32) return batch_prepare<float>(dims, sets, nsets, workspace, B, s);
+  return batch_prepare<double>(dims, sets, nsets, workspace, B, s);
+}
+
+mb_status mb_rime_batch(mb_dtype dtype, const mb_dims* dims, const mb_props* props, uint32_t options,
+                        const mb_rime_inputs* shared, const mb_batch_set* sets, int nsets, double* X2,
+                        double grad_scale, void* workspace, size_t workspace_bytes, void* stream) {
+  MB_CHECK(check_dims(dims, true));
+  MB_REQUIRE(props, "props"); MB_REQUIRE(shared, "shared inputs");
+  // the observation's inputs, with a stand-in for the per-set source arrays
+  mb_rime_inputs in = *shared;
+  const mb_dims od = batch_obs_dims(dims);
+  static const double dummy[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  in.lm = in.stokes = in.alpha = dummy;
+  in.gauss_shape = in.sersic_shape = nullptr;
+  if (options & MB_SOURCE_TILE_MASK)
+    return fail(MB_ERR_INVALID_ARG, "source tiles are chosen per set (mb_batch_set.options)");
+  MB_CHECK(check_inputs(&od, props, options, &in, nullptr));
+  if (nsets > 0) MB_REQUIRE(X2, "X2");
+  BatchPlan B;
+  MB_CHECK(batch_plan(dtype, dims, sets, nsets, B));
+  if (workspace == nullptr || workspace_bytes < B.total || (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return fail(MB_ERR_WORKSPACE, "workspace must be >= %zu bytes and 256-byte aligned (got %zu)", B.total,
+                workspace_bytes);
+  cudaStream_t s = as_stream(stream);
+  if (dtype == MB_FLOAT32) return batch_run<float>(dims, props, options, shared, nsets, X2, grad_scale, workspace, B, s);
+  return batch_run<double>(dims, props, options, shared, nsets, X2, grad_scale, workspace, B, s);
 }
 
 }  // extern "C"

@@ -8,14 +8,27 @@
 
 namespace mb {
 
+// One parameter set of a batched evaluation, as the kernels see it: the
+// set's source counts and arrays, and its regions of the batch workspace.
+template <typename T>
+struct BatchSet {
+  const T *lm, *stokes, *alpha, *gauss, *sersic;
+  const double* phi;
+  const T* bsq0;
+  double* partial;
+  T *gV, *dG;
+  double *acc_lm, *acc_stokes, *acc_alpha, *acc_gauss, *acc_sersic;
+  T *g_lm, *g_stokes, *g_alpha, *g_gauss, *g_sersic, *g_G;  // gradient outputs (any may be NULL)
+  int npsrc, ngsrc, nssrc, pad;
+};
+
 template <typename T>
 struct FusedArgs {
   // active extents and local strides
   int ntime, na, nbl, nchan, nsrc, npsrc, ngsrc, nssrc;
   int ltime, lna, lnbl, lchan, lgsrc, lssrc;
   int lw, mh, nud;
-  int t0, ch0;  // first (time, channel) unit handled by this launch
-  int sbeg;     // first source handled by the CUDA-core adjoint
+  int sbeg;     // first source handled by the CUDA-core adjoint (batched: < 0 for the set's npsrc)
   int src_tile; // requested sources per tile of the CUDA-core kernels (0: default)
   bool accumulate_in, partial_out, weights, residuals, want_grad;
   T ll, lmm, ul, um, lfreq, ufreq, lscale, mscale, gauss_scale, two_pi_over_c;
@@ -38,7 +51,13 @@ struct FusedArgs {
   // adjoint accumulators (FP64)
   double *acc_lm, *acc_stokes, *acc_alpha, *acc_gauss, *acc_sersic;
   int* err;  // device error word (bounded waits that gave up), or NULL
-  unsigned char* yop;  // (ntime * nchan) x 128 KB tensor-core operands of d chi^2 / dV, or NULL
+  // Batched evaluation (mb_rime_batch): CTA b of a launch handles unit
+  // bitems[b].y of parameter set bitems[b].x, whose source counts, source
+  // arrays, tables, partials and accumulators bsets[set] gives; NULL for a
+  // single problem.  Kernels of a launch over sets (grid.y = set) read
+  // bsets[blockIdx.y].
+  const BatchSet<T>* bsets;
+  const int2* bitems;
 };
 
 // Per-antenna data for one (time, channel) unit.

@@ -1,6 +1,7 @@
-"""Batched likelihood over many parameter sets sharing one observation:
-per-set results equal single-problem calls, graph replay equals eager
-execution, the autotuner picks a valid form per set."""
+"""Batched likelihood over many parameter sets sharing one observation
+(mb_rime_batch): per-set results equal single-problem calls and the FP64
+oracle, a batch is a fixed number of launches whatever its size, graph
+replay equals eager execution, the autotuner picks a valid form per set."""
 import numpy as np
 import pytest
 
@@ -92,3 +93,84 @@ def test_source_tiles_leave_results_unchanged(dtype, form, tile):
         for k in ('lm', 'stokes', 'gauss_shape', 'sersic_shape'):
             if ga[k].size:
                 assert np.abs(ga[k] - gb[k]).max() <= 10 * tol * max(np.abs(ga[k]).max(), 1e-30), (i, k)
+
+
+def _with_set(P, s):
+    Q = dict(P)
+    for k in ('lm', 'stokes', 'alpha', 'gauss_shape', 'sersic_shape', 'npsrc', 'ngsrc', 'nssrc'):
+        Q[k] = s[k]
+    return Q
+
+
+def _empty_set(P, npsrc=0, ngsrc=0, nssrc=0, seed=0):
+    """A set with the given counts, parameters drawn like make_sets does."""
+    from montblanc_gb300.batch import make_sets
+    s = make_sets(P, 1, seed=seed, lo=40, hi=41)[0]
+    n = npsrc + ngsrc + nssrc
+    out = {'npsrc': npsrc, 'ngsrc': ngsrc, 'nssrc': nssrc,
+           'lm': s['lm'][:n], 'stokes': s['stokes'][:n], 'alpha': s['alpha'][:n],
+           'gauss_shape': s['gauss_shape'][:, :ngsrc], 'sersic_shape': s['sersic_shape'][:, :nssrc]}
+    return out
+
+
+#: chi^2 (relative) and gradient (norm-wise relative, worst parameter) bounds
+#: against the FP64 oracle.
+ORACLE_TOL = {'double': (1e-10, 1e-9), 'float': (1e-5, 1e-3)}
+
+
+@pytest.mark.parametrize('dtype', ['double', 'float'])
+def test_batch_sets_match_oracle(dtype):
+    """Sets of one batch against the FP64 oracle (chi^2 and every gradient):
+    three generated sets, a set without sources and one with extended sources
+    only; in FP32 the sets mix the CUDA-core and TF32 split forms and source
+    tiles, so the batch runs several forward and adjoint launches."""
+    from montblanc_gb300.batch import RimeBatch, make_sets
+    from oracle import adjoint as OA
+    from oracle import rime_v4 as O
+    P = _observation()
+    sets = make_sets(P, 3, seed=11, lo=8, hi=30) + [_empty_set(P), _empty_set(P, ngsrc=3, nssrc=2, seed=2)]
+    b = RimeBatch(P, sets, dtype=dtype, want_G_grad=True)
+    if dtype == 'float':
+        b.forms = ['native', 'split_tf32', 'split_tf32', 'split_tf32', 'split_tf32']
+        b.tiles = [16, 0, 8, 0, 32]
+    x2 = b.run().cpu().numpy()
+    tx2, tg = ORACLE_TOL[dtype]
+    for i, s in enumerate(sets):
+        Q = _with_set(P, s)
+        if s['npsrc'] + s['ngsrc'] + s['nssrc'] == 0:
+            ref_x2 = O.chi_sqrd(Q, O.chi_sqrd_terms(Q, np.zeros_like(P['observed_vis'])))
+            assert abs(x2[i] - ref_x2) <= tx2 * abs(ref_x2), (i, x2[i], ref_x2)
+            assert not np.any(b.set_grads(i)['G_term'] != b.set_grads(i)['G_term'])  # finite
+            continue
+        ref_x2, ref_g = OA.chi2_grad(Q)
+        assert abs(x2[i] - ref_x2) <= tx2 * abs(ref_x2), (i, x2[i], ref_x2)
+        g = b.set_grads(i)
+        for k, r in ref_g.items():
+            if r.size == 0:
+                continue
+            err = np.linalg.norm(g[k] - r) / np.linalg.norm(r)
+            assert err <= tg, (i, k, err)
+
+
+def test_batch_launches_do_not_grow_with_sets():
+    """A batch is a fixed set of launches (shared tables, one forward and one
+    adjoint launch per kernel form, the chi^2 sums, the gradients): 2 and 8
+    sets of the same forms launch the same kernels."""
+    import torch
+    from montblanc_gb300 import _cabi
+    from montblanc_gb300.batch import RimeBatch, make_sets
+    P = _observation()
+    counts = []
+    for n in (2, 8):
+        sets = make_sets(P, n, seed=3, lo=30, hi=60)
+        b = RimeBatch(P, sets, dtype='float')
+        b.forms = ['split_tf32'] * n
+        b.prepare()
+        torch.cuda.synchronize()
+        l0 = _cabi.lib.mb_kernel_launches()
+        b.run()
+        torch.cuda.synchronize()
+        counts.append(_cabi.lib.mb_kernel_launches() - l0)
+    # beam plane, path lengths, sqrt(B) table, forward, chi^2 sums, point- and
+    # extended-source adjoints, gradients
+    assert counts == [8, 8], counts
