@@ -178,10 +178,48 @@ __device__ __forceinline__ int cta_unit(FusedArgs<T>& A) {
   return it.y;
 }
 
+// Global index of local antenna a (identity unless the launch works on an
+// antenna sub-array).
+template <typename T>
+__device__ __forceinline__ int gant(const FusedArgs<T>& A, int a) {
+  return a < A.sub_n0 ? A.sub_off0 + a : A.sub_off1 + (a - A.sub_n0);
+}
+
+// Local index of global antenna p in this launch's sub-array, or -1.
+template <typename T>
+__device__ __forceinline__ int lant(const FusedArgs<T>& A, int p) {
+  if (A.sub_blk == 0) return p;
+  const int b = p / A.sub_blk;
+  if (b == A.sub_i) return p - A.sub_off0;
+  if (b == A.sub_j) return A.sub_n0 + (p - A.sub_off1);
+  return -1;
+}
+
+// Does this launch own baseline (p, q) of valid global antennas?  Every
+// baseline has exactly one owner among a call's sub-arrays.
+template <typename T>
+__device__ __forceinline__ bool owns(const FusedArgs<T>& A, int p, int q) {
+  if (A.sub_blk == 0) return true;
+  const int bp = p / A.sub_blk, bq = q / A.sub_blk;
+  if (bp != bq) return min(bp, bq) == A.sub_i && max(bp, bq) == A.sub_j;
+  return (bp == A.sub_i && (A.sub_diag & 1)) || (bp == A.sub_j && (A.sub_diag & 2));
+}
+
+// Baseline (p, q) of global antennas as local antennas of this launch:
+// true if both are valid and the launch owns the baseline.
+template <typename T>
+__device__ __forceinline__ bool local_baseline(const FusedArgs<T>& A, int p, int q, int& pl, int& ql) {
+  if (p < 0 || p >= A.na_glob || q < 0 || q >= A.na_glob || !owns(A, p, q)) return false;
+  pl = lant(A, p);
+  ql = lant(A, q);
+  return true;
+}
+
 template <typename T>
 __device__ void load_antennas(const FusedArgs<T>& A, int t, int ch, AntInfo<T>* sa) {
   for (int a = threadIdx.x; a < A.na; a += blockDim.x) {
-    size_t ta = size_t(t) * A.lna + a;
+    const int g = gant(A, a);
+    size_t ta = size_t(t) * A.lna + g;
     AntInfo<T> ai;
     if (sizeof(T) == 8) {
       double s_, c_; sincos(double(A.pa[ta]), &s_, &c_); ai.sin_pa = T(s_); ai.cos_pa = T(c_);
@@ -190,7 +228,7 @@ __device__ void load_antennas(const FusedArgs<T>& A, int t, int ch, AntInfo<T>* 
     }
     size_t tac = ta * A.lchan + ch;
     ai.pe_l = A.pe[2 * tac]; ai.pe_m = A.pe[2 * tac + 1];
-    size_t ac = size_t(a) * A.lchan + ch;
+    size_t ac = size_t(g) * A.lchan + ch;
     ai.sc_l = A.sc[2 * ac]; ai.sc_m = A.sc[2 * ac + 1];
     ai.u = A.uvw[3 * ta]; ai.v = A.uvw[3 * ta + 1]; ai.w = A.uvw[3 * ta + 2];
     sa[a] = ai;
@@ -240,11 +278,11 @@ template <typename T>
 __device__ __forceinline__ Cx<T> phase_term(const FusedArgs<T>& A, int t, int s, int a, T f, double nu_over_c) {
   double phi;
   if (A.phi != nullptr) {
-    phi = A.phi[(size_t(t) * A.nsrc + s) * A.na + a];
+    phi = A.phi[(size_t(t) * A.nsrc + s) * A.na_glob + gant(A, a)];
   } else {  // no table: the same FP64 path length, formed in place
     double l = A.lm[2 * s], m = A.lm[2 * s + 1];
     double n = sqrt(1.0 - l * l - m * m) - 1.0;
-    const T* p = A.uvw + 3 * (size_t(t) * A.lna + a);
+    const T* p = A.uvw + 3 * (size_t(t) * A.lna + gant(A, a));
     phi = l * double(p[0]) + m * double(p[1]) + n * double(p[2]);
   }
   if (sizeof(T) == 8) return phase_from_phi<T>(phi, double(f));
@@ -339,7 +377,7 @@ __device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const J
   Jones<T>* sG = scratch;
   Jones<T>* sdG = scratch + A.na;
   for (int a = threadIdx.x; a < A.na; a += blockDim.x) {
-    sG[a] = jldg<T>(A.G + 8 * ((size_t(t) * A.lna + a) * A.lchan + ch));
+    sG[a] = jldg<T>(A.G + 8 * ((size_t(t) * A.lna + gant(A, a)) * A.lchan + ch));
     if (A.want_grad) sdG[a] = jzero<T>();
   }
   __syncthreads();
@@ -355,7 +393,16 @@ __device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const J
       size_t tbl = size_t(t) * A.lnbl + bl;
       int p = A.ant1[tbl], q = A.ant2[tbl];
       size_t vidx = tbl * A.lchan + ch;
-      if (p < 0 || p >= A.na || q < 0 || q >= A.na) {  // invalid antenna index: NaN output
+      const bool valid = p >= 0 && p < A.na_glob && q >= 0 && q < A.na_glob;
+      // with antenna sub-arrays, each baseline is written by the launch that
+      // owns it (invalid ones by the first), in local antenna indices
+      const bool mine = valid ? owns(A, p, q) : (A.sub_blk == 0 || (A.sub_i == 0 && A.sub_j == 1));
+      if (mine && valid) {
+        p = lant(A, p);
+        q = lant(A, q);
+      }
+      if (!mine) {
+      } else if (!valid) {  // invalid antenna index: NaN output
         const T nan = T(NAN);
         if (A.model_vis) jstore(A.model_vis + 8 * vidx, Jones<T>{{nan, nan}, {nan, nan}, {nan, nan}, {nan, nan}});
         if (A.chi2 && !A.partial_out) A.chi2[vidx] = nan;
@@ -419,8 +466,11 @@ __device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const J
   if (threadIdx.x == 0) A.partial[unit] = tot;
   if (A.want_grad) {
     __syncthreads();
-    for (int a = threadIdx.x; a < A.na; a += blockDim.x)
-      jstore(A.dG + 8 * ((size_t(t) * A.na + a) * A.nchan + ch), sdG[a]);
+    for (int a = threadIdx.x; a < A.na; a += blockDim.x) {
+      T* dst = A.dG + 8 * ((size_t(t) * A.na_glob + gant(A, a)) * A.nchan + ch);
+      if (A.sub_blk == 0) jstore(dst, sdG[a]);
+      else atomic_add_jones(reinterpret_cast<Jones<T>*>(dst), sdG[a]);  // antenna in several sub-arrays
+    }
   }
 }
 
@@ -846,9 +896,9 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
       if (g + 1 < nstages && A.phi != nullptr) {  // the next stage's source terms into L1
         const int sn = s0 + NSRC + sl;
         if (sn < A.npsrc) {
-          const double* pn = A.phi + (size_t(t) * A.nsrc + sn) * A.na;
-          if (lane < A.na) tc::prefetch_l1(pn + lane);
-          if (lane + 32 < A.na) tc::prefetch_l1(pn + lane + 32);
+          const double* pn = A.phi + (size_t(t) * A.nsrc + sn) * A.na_glob;
+          if (lane < A.na) tc::prefetch_l1(pn + gant(A, lane));
+          if (lane + 32 < A.na) tc::prefetch_l1(pn + gant(A, lane + 32));
           if (lane == 0) {
             tc::prefetch_l1(A.lm + 2 * sn);
             if (A.bsq0) tc::prefetch_l1(A.bsq0 + kBsqVals * (size_t(sn) * A.ntime + t));
@@ -1419,8 +1469,8 @@ __global__ void __launch_bounds__(AdjTile<T>::THREADS) coh_adj_kernel(FusedArgs<
   __syncthreads();
   for (int bl = threadIdx.x; bl < A.nbl; bl += blockDim.x) {
     size_t tbl = size_t(t) * A.lnbl + bl;
-    int p = A.ant1[tbl], q = A.ant2[tbl];
-    if (p < 0 || p >= A.na || q < 0 || q >= A.na) continue;
+    int p, q;
+    if (!local_baseline(A, A.ant1[tbl], A.ant2[tbl], p, q)) continue;
     Jones<T> g = jload<T>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch));
     if (AdjTile<T>::FULL_Y) {
       // baseline (p, q): Y_pq += gV, Y_qp += gV^H (p == q: both terms)
@@ -1659,8 +1709,8 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
     __syncthreads();
     for (int bl = tid; bl < A.nbl; bl += blockDim.x) {
       const size_t tbl = size_t(t) * A.lnbl + bl;
-      const int p = A.ant1[tbl], q = A.ant2[tbl];
-      if (p < 0 || p >= na || q < 0 || q >= na) continue;
+      int p, q;
+      if (!local_baseline(A, A.ant1[tbl], A.ant2[tbl], p, q)) continue;
       const Jones<float> g = jload<float>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch));
       atomic_add_jones(reinterpret_cast<Jones<float>*>(ybase + size_t(p) * yrow) + q, g);
       atomic_add_jones(reinterpret_cast<Jones<float>*>(ybase + size_t(q) * yrow) + p, jherm(g));
@@ -1742,7 +1792,8 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
         const int sn0 = tile_of(g + kTaGroups) * kTaKappa;
 #pragma unroll
         for (int u = 0; u < kTaItems; ++u)
-          if (sn0 + 4 * i + u < A.npsrc) tc::prefetch_l1(A.phi + (size_t(t) * A.nsrc + sn0 + 4 * i + u) * A.na + a);
+          if (sn0 + 4 * i + u < A.npsrc)
+            tc::prefetch_l1(A.phi + (size_t(t) * A.nsrc + sn0 + 4 * i + u) * A.na_glob + gant(A, a));
       }
       if (ct < kTaKappa && g + 2 * kTaGroups < ntiles) {  // the source terms' table entries, two tiles ahead
         const int s = tile_of(g + 2 * kTaGroups) * kTaKappa + ct;
@@ -2080,6 +2131,51 @@ __global__ void sum_partials_sets_kernel(const BatchSet<T>* __restrict__ sets, i
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
+// Antenna sub-arrays.  The fused kernels hold one (time, channel) unit's
+// pair sums (or, in the adjoint, its matrix of d chi^2 / dV) for at most
+// kSubMaxNa antennas: the tensor-core kernels' 128-row MMA tile and the
+// CUDA-core kernels' shared memory.  A larger array is split into blocks of
+// kSubBlock antennas and evaluated as one launch per pair of blocks I < J on
+// the antennas of both; that launch owns the baselines between I and J, and
+// those within I when J = I + 1 and within J for the last pair, so each
+// baseline is summed, written and differentiated exactly once.  Per-antenna
+// work is repeated in each launch that holds the antenna (nb - 1 times for
+// nb blocks); chi^2 partials are kept per launch and dchi^2/dG is summed
+// over them.
+constexpr int kSubMaxNa = 64;
+constexpr int kSubBlock = 32;
+
+int sub_blocks(int na) { return (na + kSubBlock - 1) / kSubBlock; }
+int sub_count(int na) {
+  if (na <= kSubMaxNa) return 1;
+  const int nb = sub_blocks(na);
+  return nb * (nb - 1) / 2;
+}
+
+// Arguments of sub-array launch k (of sub_count(A.na)) over `units` units.
+template <typename T>
+FusedArgs<T> sub_args(const FusedArgs<T>& A, int k, int units) {
+  if (A.na_glob <= kSubMaxNa) return A;
+  const int na = A.na_glob, nb = sub_blocks(na);
+  int I = 0, r = k;  // launch k is the k-th pair (I, J), I < J, in row-major order
+  while (r >= nb - 1 - I) {
+    r -= nb - 1 - I;
+    ++I;
+  }
+  const int J = I + 1 + r;
+  FusedArgs<T> S = A;
+  S.sub_blk = kSubBlock;
+  S.sub_i = I;
+  S.sub_j = J;
+  S.sub_off0 = I * kSubBlock;
+  S.sub_off1 = J * kSubBlock;
+  S.sub_n0 = std::min(kSubBlock, na - S.sub_off0);
+  S.na = S.sub_n0 + std::min(kSubBlock, na - S.sub_off1);
+  S.sub_diag = (J == I + 1 ? 1 : 0) | (I == nb - 2 && J == nb - 1 ? 2 : 0);
+  if (A.partial) S.partial = A.partial + size_t(k) * units;
+  return S;
+}
+
 struct WsLayout {
   size_t phi, plane, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, err, total;
 };
@@ -2094,7 +2190,7 @@ WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_gra
   L.phi = take(nt * ns * na * 8);
   L.plane = take(nc * size_t(d->beam_lw.local_size) * d->beam_mh.local_size * kPlaneVals * es);
   L.bsq0 = take(dtype == MB_FLOAT32 ? ns * nt * kBsqVals * es : 0);
-  L.partial = take(nt * nc * 8);
+  L.partial = take(nt * nc * size_t(sub_count(int(na))) * 8);
   L.gV = take(want_grad ? nt * nbl * nc * 8 * es : 0);
   L.dG = take(want_grad ? nt * na * nc * 8 * es : 0);
   L.acc_lm = take(want_grad ? ns * 2 * 8 : 0);
@@ -2119,6 +2215,8 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.lw = d->beam_lw.local_size; A.mh = d->beam_mh.local_size; A.nud = d->beam_nud.local_size;
   A.sbeg = 0;
   A.bsets = nullptr; A.bitems = nullptr;
+  A.na_glob = A.na; A.sub_blk = 0; A.sub_i = A.sub_j = 0; A.sub_n0 = A.na;
+  A.sub_off0 = A.sub_off1 = 0; A.sub_diag = 3;
   A.accumulate_in = d->nsrc.lower_extent > 0;
   A.partial_out = d->nsrc.upper_extent < d->nsrc.global_size;
   A.weights = options & MB_APPLY_WEIGHTS;
@@ -2344,33 +2442,41 @@ mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* 
     return MB_OK;
   }
   MB_CHECK(launch_prep(A, ws, L, stream));
-  bool done = false;
-  if constexpr (sizeof(T) == 4) {
-    if (mode != MB_MODE_NATIVE) {
-      MB_CHECK(run_tc_fwd(A, mode, units, stream));
-      done = true;
+  const int nsub = sub_count(A.na);
+  // sub-arrays add their dchi^2/dG terms into it
+  if (nsub > 1 && A.want_grad && A.dG)
+    MB_CUDA(cudaMemsetAsync(A.dG, 0, size_t(A.ntime) * A.na * A.nchan * 8 * sizeof(T), stream));
+  for (int k = 0; k < nsub; ++k) {
+    const FusedArgs<T> Ak = sub_args(A, k, units);
+    bool done = false;
+    if constexpr (sizeof(T) == 4) {
+      if (mode != MB_MODE_NATIVE) {
+        MB_CHECK(run_tc_fwd(Ak, mode, units, stream));
+        done = true;
+      }
     }
+    if (!done) MB_CHECK(run_fwd(Ak, units, stream));
   }
-  if (!done) MB_CHECK(run_fwd(A, units, stream));
   {
     KernelScope ks_("sum_partials_kernel", stream);
-    sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units, A.weights ? 1.0 : A.inv_sigma2, X2);
+    sum_partials_kernel<<<1, 1024, 0, stream>>>(A.partial, units * nsub, A.weights ? 1.0 : A.inv_sigma2, X2);
   }
   return check_launch("sum_partials_kernel");
 }
 
 // Split-precision adjoint: point sources on the tensor cores, extended
 // sources on the CUDA cores (same FP64 accumulators).
-mb_status launch_tc_adjoint(FusedArgs<float> A, cudaStream_t stream) {
-  if (A.na > 64)
-    return fail(MB_ERR_UNSUPPORTED, "split-precision modes handle up to 64 antennas (got %d)", A.na);
+mb_status launch_tc_adjoint(const FusedArgs<float>& A, cudaStream_t stream) {
   const int units = A.ntime * A.nchan;
   // the error word is the forward's (cleared there): an adjoint after a
   // forward whose waits gave up does no work and keeps reporting it
-  if (A.npsrc > 0) MB_CHECK(run_tc_adj(A, units, stream));
-  if (A.nsrc > A.npsrc) {
-    A.sbeg = A.npsrc;
-    MB_CHECK(run_adj(A, true, units, stream));
+  for (int k = 0, nsub = sub_count(A.na); k < nsub; ++k) {
+    FusedArgs<float> Ak = sub_args(A, k, units);
+    if (Ak.npsrc > 0) MB_CHECK(run_tc_adj(Ak, units, stream));
+    if (Ak.nsrc > Ak.npsrc) {
+      Ak.sbeg = Ak.npsrc;
+      MB_CHECK(run_adj(Ak, true, units, stream));
+    }
   }
   return MB_OK;
 }
@@ -2388,7 +2494,8 @@ mb_status launch_adjoint(const FusedArgs<T>& A, mb_mode mode, double grad_scale,
       done_sources = true;
     }
   }
-  if (units > 0 && A.nsrc > 0 && !done_sources) MB_CHECK(run_adj(A, false, units, stream));
+  if (units > 0 && A.nsrc > 0 && !done_sources)
+    for (int k = 0, nsub = sub_count(A.na); k < nsub; ++k) MB_CHECK(run_adj(sub_args(A, k, units), false, units, stream));
   size_t total = size_t(A.nsrc) * 2 + size_t(A.nsrc) * A.ntime + 3 * size_t(A.ngsrc) + 3 * size_t(A.nssrc) +
                  size_t(A.ntime) * A.na * A.nchan;
   if (total > 0) {
@@ -2452,8 +2559,8 @@ mb_status batch_plan(mb_dtype dtype, const mb_dims* d, const mb_batch_set* sets,
       return fail(MB_ERR_INVALID_ARG, "set %d: mode %u", i, s.mode);
     if (s.mode != MB_MODE_NATIVE && dtype != MB_FLOAT32)
       return fail(MB_ERR_UNSUPPORTED, "set %d: split-precision modes take FLOAT32 data", i);
-    if (s.mode != MB_MODE_NATIVE && na > 64)
-      return fail(MB_ERR_UNSUPPORTED, "set %d: split-precision modes handle up to 64 antennas (got %zu)", i, na);
+    if (na > size_t(kSubMaxNa))
+      return fail(MB_ERR_UNSUPPORTED, "batched calls handle up to %d antennas (got %zu)", kSubMaxNa, na);
     if (s.options & ~MB_SOURCE_TILE_MASK)
       return fail(MB_ERR_INVALID_ARG, "set %d: options may only hold source-tile bits (0x%x)", i, s.options);
     if (s.reserved != 0) return fail(MB_ERR_INVALID_ARG, "set %d: reserved must be 0", i);

@@ -29,6 +29,13 @@ struct FusedArgs {
   int ltime, lna, lnbl, lchan, lgsrc, lssrc;
   int lw, mh, nud;
   int sbeg;     // first source handled by the CUDA-core adjoint (batched: < 0 for the set's npsrc)
+  // Antenna sub-array of this launch (arrays above 64 antennas): na local
+  // antennas, the first sub_n0 of them global sub_off0 + a, the others
+  // global sub_off1 + (a - sub_n0); blocks of sub_blk antennas, this launch
+  // owning the baselines between blocks sub_i and sub_j, and those within
+  // sub_i (sub_diag bit 0) and within sub_j (bit 1).  sub_blk = 0: the
+  // whole array (local = global).  na_glob: the call's active antennas.
+  int na_glob, sub_blk, sub_i, sub_j, sub_n0, sub_off0, sub_off1, sub_diag;
   int src_tile; // requested sources per tile of the CUDA-core kernels (0: default)
   bool accumulate_in, partial_out, weights, residuals, want_grad;
   T ll, lmm, ul, um, lfreq, ufreq, lscale, mscale, gauss_scale, two_pi_over_c;

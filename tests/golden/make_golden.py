@@ -308,6 +308,42 @@ def case_displaced_gradients(only=None):
         print(name, 'displaced gradients added')
 
 
+#: Arrays wider than the fused kernels' 64-antenna tile, evaluated as
+#: antenna sub-arrays: 128 antennas (four blocks of 32) and 75 antennas (a
+#: ragged last block of 11), with weights, flags and all three source types.
+WIDE = (
+    ('wide_na128', dict(ntime=2, na=128, nchan=3, npsrc=24, ngsrc=6, nssrc=3)),
+    ('wide_na75', dict(ntime=3, na=75, nchan=2, npsrc=16, ngsrc=4, nssrc=4)),
+)
+
+
+def case_wide_arrays(only=None):
+    """The reference's forward and the oracle's FP64 gradient (at the truth
+    and at displaced source positions) on the WIDE problems."""
+    for k, (name, shape) in enumerate(WIDE):
+        if only and name not in only:
+            continue
+        P = to_f32_exact(synth.make_problem(**shape, seed=BENCH_SEED + 40 + k, beam_shape=(24, 24, 8),
+                                            use_weight_vector=True, random_weights=True, flag_fraction=0.05))
+        model = reference_outputs_batched(P)['vis_out']
+        synth.add_noise(P, model, sigma=0.1, seed=BENCH_SEED + 50 + k)
+        P = to_f32_exact(P)
+        out = reference_outputs_batched(P)
+        x2g, grads = oracle_gradient(P)
+        for g, v in grads.items():
+            out['grad_' + g] = v
+        out['grad_X2'] = np.float64(x2g)
+        rng = np.random.default_rng(BENCH_SEED + 60 + k)
+        P2 = dict(P)
+        P2['lm'] = (P['lm'] + rng.normal(0.0, DISPLACEMENT, P['lm'].shape)).astype(np.float32).astype(np.float64)
+        _, dgrads = oracle_gradient(P2)
+        out['displaced_lm'] = P2['lm'].astype(np.float32)
+        for g, v in dgrads.items():
+            out['displaced_grad_' + g] = v
+        keep = tuple(g for g in out if g.startswith(('grad_', 'displaced_')))
+        save(name, P, out, keep=keep)
+
+
 def load_fixture(z):
     """Problem dict (float64 / complex128) and outputs of a fixture's arrays."""
     P, out = {}, {}
@@ -346,3 +382,5 @@ if __name__ == '__main__':
     if not args.displaced_only:
         case_sampled_units(only)
     case_displaced_gradients(only)
+    if not args.displaced_only:
+        case_wide_arrays(only)
