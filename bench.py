@@ -65,10 +65,10 @@ NCU_LIMITER = {
 # time step run together and share them in L2).
 NCU_DRAM = {
     # kernel: (bytes per unit, bytes per (time, source, antenna)); the
-    # profile_point launch moved 334.5 MB (forward) and 353.0 MB (adjoint)
+    # profile_point launch moved 337.5 MB (forward) and 217.6 MB (adjoint)
     # over 2048 units and 32 x 4050 x 64 FP64 path lengths (66.4 MB)
     'coh_tc_fwd_kernel': (145.1e3, 8.0),
-    'coh_tc_adj_kernel': (139.9e3, 8.0),
+    'coh_tc_adj_kernel': (73.8e3, 8.0),
 }
 
 
