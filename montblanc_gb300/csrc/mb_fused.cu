@@ -703,24 +703,32 @@ __device__ __forceinline__ float fold_carry(float* hi, float x) {
 // col) * 2 + re/im) split into a per-lane part and a part in b and j:
 //   b >= a:  ku + 8 b + 2 j,  ku = 8 (a na - a (a - 1) / 2 - a) + 4 i + h
 //   b <  a:  8 R_b + kl + 4 j,  kl = 8 a + 2 i + h,  R_b = b na - b (b - 1) / 2 - b
-__device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, bool carry) {
+// PACK (at most 32 antennas, two channels per CTA): rows 64 c + 2 a + i and
+// columns 64 c + 2 b + j hold channel c; only its diagonal block is
+// drained, into the pair accumulators of channel c (c npairs Jones on).
+template <bool PACK>
+__device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, bool carry, int nch) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int q = warp & 3, jw = warp >> 2;  // lane quarter, and the warp's index among its 3 warps
-  const int r = 32 * q + lane, a = r >> 1, i = r & 1;
+  const int r = 32 * q + lane, i = r & 1;
+  const int c = PACK ? (r >> 6) : 0, a = PACK ? ((r >> 1) & 31) : (r >> 1);
   const int na = A.na;
-  const bool row_ok = a < na;
+  const bool row_ok = a < na && c < nch;
+  if (PACK) sVf += size_t(c) * (na * (na + 1) / 2) * 8;
   const int dmax = (na - 1) / 2 + ((na % 2 == 0 && a < na / 2) ? 1 : 0);
   const int up_hi = row_ok ? min(a + dmax, na - 1) : -1;
   const int wrap_end = row_ok ? a + dmax - na : -1;
   const int ku0 = 8 * (a * na - (a * (a - 1)) / 2 - a) + 4 * i;
   const int kl0 = 8 * a + 2 * i;
-  // 8 tasks (matrix h, column block blk) per lane quarter, dealt to its warps
+  // 8 tasks (matrix h, column block blk of 16 antennas) per lane quarter
+  // (PACK: 4, the blocks of the quarter's channel), dealt to its warps
+  constexpr int kTasks = PACK ? 4 : 8;
 #pragma unroll 1
-  for (int task = jw; task < 8; task += 3) {
-    const int h = task >> 2, blk = task & 3;
+  for (int task = jw; task < kTasks; task += 3) {
+    const int h = PACK ? task >> 1 : task >> 2, blk = PACK ? task & 1 : task & 3;
     const int ku = ku0 + h, kl = kl0 + h;
     const float sgn = h ? -1.f : 1.f;
-    const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(h * 128);
+    const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(h * 128) + uint32_t(PACK ? 64 * c : 0);
     const int b_lo = 16 * blk;
     const bool need = (max(a, b_lo) <= min(up_hi, b_lo + 15)) || (wrap_end >= b_lo);
     if (!__any_sync(0xffffffffu, need)) continue;  // warp-uniform: the loads are collective
@@ -807,7 +815,10 @@ __device__ __forceinline__ SrcInfo<float> point_source_stokes(const FusedArgs<fl
   return si;
 }
 
-template <int MODE, bool BATCHED>
+// PACK (at most 32 antennas): a CTA takes the unit pair (t, 2k), (t, 2k + 1);
+// operand rows 64 c + 2 a + i hold channel c (producer lane a, rep c), so one
+// MMA sequence and one drain pass serve both channels.
+template <int MODE, bool BATCHED, bool PACK>
 __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float> A_in, SmemPlan S, TcPlan P) {
   constexpr int kRowBytes = TcGeom<MODE>::kRowBytes;
   constexpr int KAPPA = TcGeom<MODE>::kSlots;  // source slots per stage
@@ -834,18 +845,29 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   FusedArgs<float> A = A_in;
-  int unit = blockIdx.x;
-  if constexpr (BATCHED) unit = cta_unit(A);
-  const int t = unit / A.nchan, ch = unit - t * A.nchan;
+  int cta = blockIdx.x;
+  if constexpr (BATCHED) cta = cta_unit(A);
+  constexpr int NCH = PACK ? 2 : 1;  // channels per CTA
+  int t, ch, nch = 1;                // time, first channel, channels of this CTA
+  if (PACK) {
+    const int npc = (A.nchan + 1) / 2;
+    t = cta / npc;
+    ch = 2 * (cta - t * npc);
+    nch = min(2, A.nchan - ch);
+  } else {
+    t = cta / A.nchan;
+    ch = cta - t * A.nchan;
+  }
+  const int unit = t * A.nchan + ch;  // the first channel's unit; the second is unit + 1
   if (tid == 0) *abort_flag = A.err ? *reinterpret_cast<volatile int*>(A.err) : 0;
   __syncthreads();
   if (*abort_flag) {  // an earlier CTA timed out: do no work
-    if (tid == 0) A.partial[unit] = double(NAN);
+    if (tid < nch) A.partial[unit + tid] = double(NAN);
     return;
   }
   __syncthreads();
-  load_antennas(A, t, ch, sa);
-  for (int i = tid; i < S.npairs; i += blockDim.x) sV[i] = jzero<float>();
+  for (int c = 0; c < nch; ++c) load_antennas(A, t, ch + c, sa + c * A.na);
+  for (int i = tid; i < NCH * S.npairs; i += blockDim.x) sV[i] = jzero<float>();
   // the stage buffers' unused slots are read by the MMAs as zeros
   for (int i = tid; i < int(kTcStages * 2 * L::kMatBytes / 16); i += blockDim.x)
     reinterpret_cast<uint4*>(stage)[i] = make_uint4(0u, 0u, 0u, 0u);
@@ -869,12 +891,19 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   tc::fence_after_thread_sync();
   const uint32_t tmem = *tmem_slot;
 
-  const float f = A.freq[ch];
-  const double nu_over_c = double(f) / kLightSpeed;
-  const ChanPos<float> cp = chan_pos<float>(f, A.lfreq, A.ufreq, A.nud);
+  float fc[NCH], log2_ratio[NCH];
+  double nu_over_c[NCH];
+  ChanPos<float> cp[NCH];
+#pragma unroll
+  for (int c = 0; c < NCH; ++c) {
+    const int chc = min(ch + c, A.nchan - 1);
+    fc[c] = A.freq[chc];
+    nu_over_c[c] = double(fc[c]) / kLightSpeed;
+    cp[c] = chan_pos<float>(fc[c], A.lfreq, A.ufreq, A.nud);
+    log2_ratio[c] = log2f(fc[c] / A.ref_freq[chc]);
+  }
   const int nstages = (A.npsrc + NSRC - 1) / NSRC;
   const int group = P.group;
-  const float log2_ratio = log2f(f / A.ref_freq[ch]);
   const uint32_t wlim = g_pipe_wait_limit;
   bool bad = false;
 
@@ -909,21 +938,27 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
       if (!bad) {
         unsigned char* hi = stage + size_t(slot) * 2 * L::kMatBytes;
         unsigned char* lo = hi + L::kMatBytes;
-        // the source's terms, the same for both antennas of the lane
+        // the source's terms, the same for both antennas of the lane (PACK:
+        // per channel)
         SrcInfo<float> src;
-        if (sl < ns) src = point_source_info(A, t, ch, s0 + sl, log2_ratio);
+        if (!PACK && sl < ns) src = point_source_info(A, t, ch, s0 + sl, log2_ratio[0]);
 #pragma unroll
         for (int rep = 0; rep < 2; ++rep) {
-          const int a = lane + 32 * rep;
+          const int c = PACK ? rep : 0;
+          const int a = PACK ? lane : lane + 32 * rep;  // antenna
+          const int ra = lane + 32 * rep;               // its rows 2 ra, 2 ra + 1
           Jones<float> J = jzero<float>();
-          if (a < A.na && sl < ns) J = compute_jones(A, t, s0 + sl, a, src, sa[a], f, nu_over_c, cp, ch);
+          if (a < A.na && sl < ns && c < nch) {
+            if (PACK) src = point_source_info(A, t, ch + c, s0 + sl, log2_ratio[c]);
+            J = compute_jones(A, t, s0 + sl, a, src, sa[c * A.na + a], fc[c], nu_over_c[c], cp[c], ch + c);
+          }
           // row 2a holds J00, J01; row 2a + 1 holds J10, J11
           const Cx<float> r0a = i0 ? J.c : J.a, r0b = i0 ? J.d : J.b;
           const Cx<float> r1a = i0 ? J.a : J.c, r1b = i0 ? J.b : J.d;
-          L::put2(hi, lo, 2 * a + i0, 2 * sl, r0a.r, r0b.r);
-          L::put2(hi, lo, 2 * a + i0, 2 * KAPPA + 2 * sl, r0a.i, r0b.i);
-          L::put2(hi, lo, 2 * a + 1 - i0, 2 * sl, r1a.r, r1b.r);
-          L::put2(hi, lo, 2 * a + 1 - i0, 2 * KAPPA + 2 * sl, r1a.i, r1b.i);
+          L::put2(hi, lo, 2 * ra + i0, 2 * sl, r0a.r, r0b.r);
+          L::put2(hi, lo, 2 * ra + i0, 2 * KAPPA + 2 * sl, r0a.i, r0b.i);
+          L::put2(hi, lo, 2 * ra + 1 - i0, 2 * sl, r1a.r, r1b.r);
+          L::put2(hi, lo, 2 * ra + 1 - i0, 2 * KAPPA + 2 * sl, r1a.i, r1b.i);
         }
         tc::fence_proxy_async_smem();
         tc::mbar_arrive(full + slot);
@@ -934,7 +969,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
         if (!bad) bad = !tc::mbar_wait(accfull, ((g / group) - 1) & 1, wlim);
         tc::fence_after_thread_sync();
         bad = __any_sync(0xffffffffu, bad);  // the drain's TMEM loads are warp-collective
-        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), true);
+        if (!bad) tc_drain<PACK>(A, tmem, reinterpret_cast<float*>(sV), true, nch);
         tc::fence_before_thread_sync();
         if (!bad) tc::mbar_arrive(accfree);
       }
@@ -943,7 +978,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
       if (!bad) bad = !tc::mbar_wait(accfull, ((nstages - 1) / group) & 1, wlim);
       tc::fence_after_thread_sync();
       bad = __any_sync(0xffffffffu, bad);
-      if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), false);
+      if (!bad) tc_drain<PACK>(A, tmem, reinterpret_cast<float*>(sV), false, nch);
       tc::fence_before_thread_sync();
       if (!bad) tc::mbar_arrive(accfree);
     }
@@ -960,7 +995,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
         if (!bad) bad = !tc::mbar_wait(accfull, ((g / group) - 1) & 1, wlim);
         tc::fence_after_thread_sync();
         bad = __any_sync(0xffffffffu, bad);
-        if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), true);
+        if (!bad) tc_drain<PACK>(A, tmem, reinterpret_cast<float*>(sV), true, nch);
         tc::fence_before_thread_sync();
         if (!bad) tc::mbar_arrive(accfree);
       }
@@ -1013,7 +1048,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
       if (!bad) bad = !tc::mbar_wait(accfull, ((nstages - 1) / group) & 1, wlim);
       tc::fence_after_thread_sync();
       bad = __any_sync(0xffffffffu, bad);
-      if (!bad) tc_drain(A, tmem, reinterpret_cast<float*>(sV), false);
+      if (!bad) tc_drain<PACK>(A, tmem, reinterpret_cast<float*>(sV), false, nch);
       tc::fence_before_thread_sync();
       if (!bad) tc::mbar_arrive(accfree);
     }
@@ -1029,31 +1064,35 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   if (warp == kTcProducerWarps) tc::tmem_dealloc(tmem, kTcCols);
   const bool aborted = *abort_flag != 0;
 
-  // ---- extended sources on the CUDA cores --------------------------------
+  // ---- extended sources on the CUDA cores, then the epilogue, per channel --
   // they accumulate with FP32 low parts in the stage region
-  {
-    float* vlo = reinterpret_cast<float*>(sVlo);
-    for (int i = tid; i < S.npairs * 8; i += blockDim.x) vlo[i] = 0.f;
-  }
-  __syncthreads();
-  const float kg = A.gauss_scale * f, ks = A.two_pi_over_c * f;
-  for (int s0 = A.npsrc; s0 < A.nsrc && !aborted;) {
-    const int s1 = min(s0 + S.st, A.nsrc), ns = s1 - s0;
-    load_sources(A, t, ch, s0, ns, ss);
+  for (int c = 0; c < nch; ++c) {
+    Jones<float>* sVc = sV + c * S.npairs;
+    const AntInfo<float>* sac = sa + c * A.na;
+    {
+      float* vlo = reinterpret_cast<float*>(sVlo);
+      for (int i = tid; i < S.npairs * 8; i += blockDim.x) vlo[i] = 0.f;
+    }
     __syncthreads();
-    produce_jones(A, S, t, ch, s0, ns, ss, sa, sJ, cp);
+    const float kg = A.gauss_scale * fc[c], ks = A.two_pi_over_c * fc[c];
+    for (int s0 = A.npsrc; s0 < A.nsrc && !aborted;) {
+      const int s1 = min(s0 + S.st, A.nsrc), ns = s1 - s0;
+      load_sources(A, t, ch + c, s0, ns, ss);
+      __syncthreads();
+      produce_jones(A, S, t, ch + c, s0, ns, ss, sac, sJ, cp[c]);
+      __syncthreads();
+      consume_pairs<float, 2, 4>(A, S, ns, ss, sac, sJ, sVc, sVlo, items, true, kg, ks);
+      __syncthreads();
+      s0 = s1;
+    }
+    for (int i = tid; i < S.npairs; i += blockDim.x) sVc[i] = jadd(sVc[i], sVlo[i]);
     __syncthreads();
-    consume_pairs<float, 2, 4>(A, S, ns, ss, sa, sJ, sV, sVlo, items, true, kg, ks);
+    epilogue(A, t, ch + c, unit + c, sVc, sJ, red);
     __syncthreads();
-    s0 = s1;
-  }
-  for (int i = tid; i < S.npairs; i += blockDim.x) sV[i] = jadd(sV[i], sVlo[i]);
-  __syncthreads();
-  epilogue(A, t, ch, unit, sV, sJ, red);
-  __syncthreads();
-  if (aborted && tid == 0) {
-    A.partial[unit] = double(NAN);
-    if (A.err) atomicExch(A.err, int(MB_ERR_TIMEOUT));
+    if (aborted && tid == 0) {
+      A.partial[unit + c] = double(NAN);
+      if (A.err) atomicExch(A.err, int(MB_ERR_TIMEOUT));
+    }
   }
 }
 
@@ -1653,14 +1692,18 @@ __device__ __forceinline__ void ta_issue_chain(bool im, uint32_t d, uint32_t ytm
   }
 }
 
-template <bool BATCHED>
+// PACK (at most 32 antennas): a CTA takes the unit pair (t, 2k), (t, 2k + 1);
+// TMEM lane 64 c + 2 a + i works on channel c, antenna a, and Y is the
+// block-diagonal matrix of both channels over 64 virtual antennas 32 c + a,
+// so one sequence of MMAs serves both channels.
+template <bool BATCHED, bool PACK>
 __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<float> A_in, TaPlan P) {
   extern __shared__ __align__(16) unsigned char smem[];
   float4* park = reinterpret_cast<float4*>(smem + P.off_park);  // [group][item][kTaPark][128 lanes]
   unsigned char* stage = smem + P.off_stage;  // [kTaGroups][kJopBytes]
   AntInfo<float>* sa = reinterpret_cast<AntInfo<float>*>(smem + P.off_ant);
-  float* sacc = reinterpret_cast<float*>(smem + P.off_acc);  // [kTaGroups][2][kTaKappa][kTaAcc]
-  TaSrc* ssrc = reinterpret_cast<TaSrc*>(smem + P.off_src);   // [kTaGroups][2][kTaKappa]
+  float* sacc = reinterpret_cast<float*>(smem + P.off_acc);  // [kTaGroups][2][NCH][kTaKappa][kTaAcc]
+  TaSrc* ssrc = reinterpret_cast<TaSrc*>(smem + P.off_src);   // [kTaGroups][2][NCH][kTaKappa]
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + P.off_bar);
   uint64_t* dfull = bars;               // [kTaGroups] MMA commit -> group (dJ in TMEM)
   uint64_t* done = dfull + kTaGroups;   // [kTaGroups] last MMAs of a group
@@ -1669,16 +1712,27 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   FusedArgs<float> A = A_in;
-  int unit = blockIdx.x;
-  if constexpr (BATCHED) unit = cta_unit(A);
-  const int t = unit / A.nchan, ch = unit - t * A.nchan;
+  int cta = blockIdx.x;
+  if constexpr (BATCHED) cta = cta_unit(A);
+  constexpr int NCH = PACK ? 2 : 1;  // channels per CTA
+  int t, ch, nch = 1;                // time, first channel, channels of this CTA
+  if (PACK) {
+    const int npc = (A.nchan + 1) / 2;
+    t = cta / npc;
+    ch = 2 * (cta - t * npc);
+    nch = min(2, A.nchan - ch);
+  } else {
+    t = cta / A.nchan;
+    ch = cta - t * A.nchan;
+  }
+  const int unit = t * A.nchan + ch;
   if (tid == 0) *abort_flag = A.err ? *reinterpret_cast<volatile int*>(A.err) : 0;
   __syncthreads();
   if (*abort_flag) return;
   __syncthreads();
 
-  load_antennas(A, t, ch, sa);
-  for (int i = tid; i < kTaGroups * 2 * kTaKappa * kTaAcc; i += blockDim.x) sacc[i] = 0.f;
+  for (int c = 0; c < nch; ++c) load_antennas(A, t, ch + c, sa + c * A.na);
+  for (int i = tid; i < kTaGroups * 2 * NCH * kTaKappa * kTaAcc; i += blockDim.x) sacc[i] = 0.f;
   if (tid == 0) {
     for (int g = 0; g < kTaGroups; ++g) {
       tc::mbar_init(dfull + g, 2);  // one commit per chain issuer
@@ -1701,17 +1755,21 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
   // for b = kp < 64 and -Im of them for b = kp - 64; the lo half (columns
   // 128-255) likewise.  The three warps of a lane quarter share the row's 8
   // runs of 32 words.
+  // PACK: virtual antennas 32 c + a, off-diagonal channel blocks zero.
   {
     unsigned char* ybase = reinterpret_cast<unsigned char*>(park);
-    const int na = A.na, yrow = kTaYRowBytes;
+    const int na = PACK ? 64 : A.na, yrow = kTaYRowBytes;
     for (int x = tid; x < na * yrow / 16; x += blockDim.x)
       reinterpret_cast<uint4*>(ybase)[x] = make_uint4(0u, 0u, 0u, 0u);
     __syncthreads();
-    for (int bl = tid; bl < A.nbl; bl += blockDim.x) {
+    for (int x = tid; x < nch * A.nbl; x += blockDim.x) {
+      const int c = PACK ? x / A.nbl : 0, bl = PACK ? x - c * A.nbl : x;
       const size_t tbl = size_t(t) * A.lnbl + bl;
       int p, q;
       if (!local_baseline(A, A.ant1[tbl], A.ant2[tbl], p, q)) continue;
-      const Jones<float> g = jload<float>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch));
+      p += 32 * c;
+      q += 32 * c;
+      const Jones<float> g = jload<float>(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch + c));
       atomic_add_jones(reinterpret_cast<Jones<float>*>(ybase + size_t(p) * yrow) + q, g);
       atomic_add_jones(reinterpret_cast<Jones<float>*>(ybase + size_t(q) * yrow) + p, jherm(g));
     }
@@ -1746,12 +1804,6 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
   __syncthreads();
   tc::fence_after_thread_sync();
 
-  const float f = A.freq[ch];
-  const double nu_over_c = double(f) / kLightSpeed;
-  const ChanPos<float> cp = chan_pos<float>(f, A.lfreq, A.ufreq, A.nud);
-  const float log2_ratio = log2f(f / A.ref_freq[ch]);
-  const float half_log_ratio = 0.5f * logf(f / A.ref_freq[ch]);
-  const float dphase = float(2.0 * kPi * nu_over_c);
   const int ntiles = (A.npsrc + kTaKappa - 1) / kTaKappa;
   const uint32_t wlim = g_pipe_wait_limit;
   // Units start their tile sweep at different tiles, so that the CTAs in
@@ -1764,29 +1816,44 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
     const int grp = warp >> 2, q = warp & 3;
     const bool issuer = q < 2 && lane == 0;  // warp q = 0 issues chain Re, q = 1 chain Im
     bool issued = false;
-    const int r = 32 * q + lane, a = r >> 1, i = r & 1;
-    const bool ant_ok = a < A.na;
-    const AntInfo<float> ai = sa[ant_ok ? a : 0];
+    // TMEM lane r = (va, i): virtual antenna va = antenna a (PACK: 32 c + a,
+    // channel c, the same for the whole warp)
+    const int r = 32 * q + lane, va = r >> 1, i = r & 1;
+    const int c = PACK ? va >> 5 : 0, a = PACK ? va & 31 : va;
+    const int chl = min(ch + c, A.nchan - 1);  // this lane's channel
+    const bool ant_ok = a < A.na && c < nch;
+    const AntInfo<float> ai = sa[c * A.na + (ant_ok ? a : 0)];
+    const float f = A.freq[chl];
+    const double nu_over_c = double(f) / kLightSpeed;
+    const ChanPos<float> cp = chan_pos<float>(f, A.lfreq, A.ufreq, A.nud);
+    const float dphase = float(2.0 * kPi * nu_over_c);
     unsigned char* hi = stage + size_t(grp) * kJopBytes;
     unsigned char* lo = hi + kJopBytes / 2;
     const BeamGeom G{A.lw, A.mh, A.nud};
-    const float* plane = A.plane ? A.plane + size_t(ch) * A.lw * A.mh * kPlaneVals : nullptr;
+    const float* plane = A.plane ? A.plane + size_t(chl) * A.lw * A.mh * kPlaneVals : nullptr;
     const uint32_t tlane = tmem + (uint32_t(32 * q) << 16) + kTaYCols + uint32_t(kTaGroupCols * grp);
     float4* mypark = park + size_t(grp) * kTaItems * kTaPark * 128 + r;
-    TaSrc* gsrc = ssrc + size_t(grp) * 2 * kTaKappa;  // this group's two tiles of source terms
-    const int ct = tid - grp * kTaGroupThreads;        // thread index within the group
-    if (ct < kTaKappa && grp < ntiles) {
-      const int s = tile_of(grp) * kTaKappa + ct;
-      if (s < A.npsrc) ta_fill_src(A, t, ch, s, log2_ratio, gsrc + ct);
+    TaSrc* gsrc = ssrc + size_t(grp) * 2 * NCH * kTaKappa;  // this group's two tiles of source terms
+    const int ct = tid - grp * kTaGroupThreads;              // thread index within the group
+    // the source terms of a tile are filled by NCH * kTaKappa threads of the
+    // group: thread ct takes source ct % kTaKappa at channel ct / kTaKappa
+    const int fc_ = ct / kTaKappa, fs_ = ct - fc_ * kTaKappa;
+    const int fch = min(ch + fc_, A.nchan - 1);
+    const float flog2 = log2f(A.freq[fch] / A.ref_freq[fch]);
+    const float fhalf_log = 0.5f * logf(A.freq[fch] / A.ref_freq[fch]);
+    const bool filler = ct < NCH * kTaKappa && fc_ < nch;
+    if (filler && grp < ntiles) {
+      const int s = tile_of(grp) * kTaKappa + fs_;
+      if (s < A.npsrc) ta_fill_src(A, t, fch, s, flog2, gsrc + ct);
     }
     bool bad = group_sync_or(grp, false);
     int k = 0;  // this group's tile count
     for (int g = grp; g < ntiles; g += kTaGroups, ++k) {
       const int s0 = tile_of(g) * kTaKappa, ns = min(kTaKappa, A.npsrc - s0);
-      const TaSrc* tsrc = gsrc + (k & 1) * kTaKappa;  // this tile's source terms
-      if (ct < kTaKappa && g + kTaGroups < ntiles) {   // the next tile's, before the staging barrier
-        const int s = tile_of(g + kTaGroups) * kTaKappa + ct;
-        if (s < A.npsrc) ta_fill_src(A, t, ch, s, log2_ratio, gsrc + ((k + 1) & 1) * kTaKappa + ct);
+      const TaSrc* tsrc = gsrc + ((k & 1) * NCH + c) * kTaKappa;  // this tile's source terms (lane's channel)
+      if (filler && g + kTaGroups < ntiles) {  // the next tile's, before the staging barrier
+        const int s = tile_of(g + kTaGroups) * kTaKappa + fs_;
+        if (s < A.npsrc) ta_fill_src(A, t, fch, s, flog2, gsrc + ((k + 1) & 1) * NCH * kTaKappa + ct);
       }
       if (ant_ok && g + kTaGroups < ntiles && A.phi) {  // the items' path lengths, a tile ahead
         const int sn0 = tile_of(g + kTaGroups) * kTaKappa;
@@ -1841,11 +1908,11 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
           mypark[(u * kTaPark + 2 * x) * 128] = make_float4(st[x][0], st[x][1], st[x][2], st[x][3]);
           mypark[(u * kTaPark + 2 * x + 1) * 128] = make_float4(st[x][4], st[x][5], st[x][6], st[x][7]);
         }
-        // row (s, k): K = (a, 0), (a, 1) hold J[0][k], J[1][k]
-        TaLayout::put2(hi, lo, 2 * sl, 2 * a, J.a.r, J.c.r);
-        TaLayout::put2(hi, lo, 2 * sl, 128 + 2 * a, J.a.i, J.c.i);
-        TaLayout::put2(hi, lo, 2 * sl + 1, 2 * a, J.b.r, J.d.r);
-        TaLayout::put2(hi, lo, 2 * sl + 1, 128 + 2 * a, J.b.i, J.d.i);
+        // row (s, k): K = (va, 0), (va, 1) hold J[0][k], J[1][k]
+        TaLayout::put2(hi, lo, 2 * sl, 2 * va, J.a.r, J.c.r);
+        TaLayout::put2(hi, lo, 2 * sl, 128 + 2 * va, J.a.i, J.c.i);
+        TaLayout::put2(hi, lo, 2 * sl + 1, 2 * va, J.b.r, J.d.r);
+        TaLayout::put2(hi, lo, 2 * sl + 1, 128 + 2 * va, J.b.i, J.d.i);
       }
       tc::fence_proxy_async_smem();
       tc::fence_before_thread_sync();
@@ -1887,7 +1954,8 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
           recv[4 * u + 2 + e] = __shfl_xor_sync(0xffffffffu, i ? v[16 + own] : v[16 + oth], 1);
         }
       // ---- chain step ------------------------------------------------------
-      float* acc = sacc + (size_t(grp) * 2 + (k & 1)) * kTaKappa * kTaAcc;
+      float* tacc = sacc + (size_t(grp) * 2 + (k & 1)) * NCH * kTaKappa * kTaAcc;  // this tile's sums
+      float* acc = tacc + c * kTaKappa * kTaAcc;                                    // the lane's channel
 #pragma unroll
       for (int u = 0; u < kTaItems; ++u) {
         const int sl = 4 * i + u;
@@ -1942,18 +2010,18 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
       if (group_sync_or(grp, bad)) { bad = true; break; }
       // flush the tile's per-source sums to the FP64 accumulators; the
       // other accumulator buffer takes the group's next tile
-      if (ct < kTaKappa) {
-        float* rr = acc + ct * kTaAcc;
-        if (ct < ns) {
-          const int sg = s0 + ct;
+      if (filler) {  // thread ct: source fs_ at channel fch
+        float* rr = tacc + ct * kTaAcc;
+        if (fs_ < ns) {
+          const int sg = s0 + fs_;
           if (rr[0] != 0.f) atomicAdd(&A.acc_lm[2 * sg], double(rr[0]));
           if (rr[1] != 0.f) atomicAdd(&A.acc_lm[2 * sg + 1], double(rr[1]));
-          const SrcInfo<float> src = point_source_stokes(A, t, ch, sg, log2_ratio);
+          const SrcInfo<float> src = point_source_stokes(A, t, fch, sg, flog2);
           // a Hermitian gB with the summed parts (all the gradients read)
           const Jones<float> gB = {{rr[2], 0.f}, {0.5f * rr[4], 0.5f * rr[5]}, {0.5f * rr[4], -0.5f * rr[5]},
                                    {rr[3], 0.f}};
           float gs[5];
-          stokes_grads(src, gB, half_log_ratio, gs);
+          stokes_grads(src, gB, fhalf_log, gs);
           double* st = &A.acc_stokes[(size_t(sg) * A.ntime + t) * 4];
 #pragma unroll
           for (int e = 0; e < 4; ++e)
@@ -2323,6 +2391,12 @@ mb_status launch_prep(const FusedArgs<T>& A, void* ws, const WsLayout& L, cudaSt
 // Kernel launchers over `grid` CTAs: a single problem's (time, channel)
 // units, or a batched launch's (set, unit) items (A.bitems).
 
+// The tensor-core kernels pack two channels per CTA when the (sub-)array has
+// at most 32 antennas (its 64 operand rows then fill the 128-row MMA tile).
+bool tc_pack(int na) { return na <= 32; }
+// CTAs of a tensor-core launch over ntime x nchan units.
+int tc_ctas(int na, int ntime, int nchan) { return tc_pack(na) ? ntime * ((nchan + 1) / 2) : ntime * nchan; }
+
 // Split-precision forward: point sources on the tensor cores, extended
 // sources on the CUDA cores in the same CTA.
 mb_status run_tc_fwd(const FusedArgs<float>& A, mb_mode mode, int grid, cudaStream_t stream) {
@@ -2354,9 +2428,10 @@ mb_status run_tc_fwd(const FusedArgs<float>& A, mb_mode mode, int grid, cudaStre
     P.off_vlo32 = P.off_stage + jbytes;
     S.off_J = P.off_stage;
     S.off_Vlo = P.off_vlo32;
-    S.off_ant = take(sizeof(AntInfo<float>) * A.na);
+    const int nch = tc_pack(A.na) ? 2 : 1;
+    S.off_ant = take(sizeof(AntInfo<float>) * A.na * nch);
     S.off_src = take(sizeof(SrcInfo<float>) * S.st);
-    S.off_V = take(vbytes);
+    S.off_V = take(vbytes * nch);
     S.off_items = take(sizeof(int) * (S.nitems + 128));
     S.off_red = take(sizeof(double) * 32);
     P.off_bar = take((2 * kTcStages + 3) * sizeof(uint64_t) + 16);
@@ -2367,15 +2442,18 @@ mb_status run_tc_fwd(const FusedArgs<float>& A, mb_mode mode, int grid, cudaStre
     return fail(MB_ERR_UNSUPPORTED, "split-precision kernel needs %zu bytes of shared memory for na=%d",
                 P.total, A.na);
   if (grid == 0) return MB_OK;
-  if (mode == MB_MODE_SPLIT_TF32) {
-    auto kern = A.bitems ? coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32, true> : coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32, false>;
-    MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
-    { KernelScope ks_("coh_tc_fwd_kernel", stream); kern<<<grid, kTcThreads, P.total, stream>>>(A, S, P); }
-  } else {
-    auto kern = A.bitems ? coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16, true> : coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16, false>;
-    MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
-    { KernelScope ks_("coh_tc_fwd_kernel", stream); kern<<<grid, kTcThreads, P.total, stream>>>(A, S, P); }
-  }
+  const bool b = A.bitems != nullptr, pk = tc_pack(A.na);
+  auto kern = mode == MB_MODE_SPLIT_TF32
+                  ? (b ? (pk ? coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32, true, true>
+                             : coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32, true, false>)
+                       : (pk ? coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32, false, true>
+                             : coh_tc_fwd_kernel<MB_MODE_SPLIT_TF32, false, false>))
+                  : (b ? (pk ? coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16, true, true>
+                             : coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16, true, false>)
+                       : (pk ? coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16, false, true>
+                             : coh_tc_fwd_kernel<MB_MODE_SPLIT_BF16, false, false>));
+  MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
+  { KernelScope ks_("coh_tc_fwd_kernel", stream); kern<<<grid, kTcThreads, P.total, stream>>>(A, S, P); }
   return check_launch("coh_tc_fwd_kernel");
 }
 
@@ -2404,12 +2482,15 @@ mb_status run_tc_adj(const FusedArgs<float>& A, int grid, cudaStream_t stream) {
   auto take = [&o](size_t bytes) { size_t r = o; o = align_up(o + bytes, 128); return r; };
   P.off_park = take(kTaParkBytes);
   P.off_stage = take(size_t(kTaGroups) * kJopBytes);
-  P.off_ant = take(sizeof(AntInfo<float>) * A.na);
-  P.off_acc = take(sizeof(float) * kTaGroups * 2 * kTaKappa * kTaAcc);
-  P.off_src = take(sizeof(TaSrc) * kTaGroups * 2 * kTaKappa);
+  const int nch = tc_pack(A.na) ? 2 : 1;
+  P.off_ant = take(sizeof(AntInfo<float>) * A.na * nch);
+  P.off_acc = take(sizeof(float) * kTaGroups * 2 * nch * kTaKappa * kTaAcc);
+  P.off_src = take(sizeof(TaSrc) * kTaGroups * 2 * nch * kTaKappa);
   P.off_bar = take(2 * kTaGroups * sizeof(uint64_t) + 16);
   P.total = o;
-  auto kern = A.bitems ? coh_tc_adj_kernel<true> : coh_tc_adj_kernel<false>;
+  const bool b = A.bitems != nullptr, pk = tc_pack(A.na);
+  auto kern = b ? (pk ? coh_tc_adj_kernel<true, true> : coh_tc_adj_kernel<true, false>)
+                : (pk ? coh_tc_adj_kernel<false, true> : coh_tc_adj_kernel<false, false>);
   MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(P.total)));
   { KernelScope ks_("coh_tc_adj_kernel", stream); kern<<<grid, kTaThreads, P.total, stream>>>(A, P); }
   return check_launch("coh_tc_adj_kernel");
@@ -2451,7 +2532,7 @@ mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* 
     bool done = false;
     if constexpr (sizeof(T) == 4) {
       if (mode != MB_MODE_NATIVE) {
-        MB_CHECK(run_tc_fwd(Ak, mode, units, stream));
+        MB_CHECK(run_tc_fwd(Ak, mode, tc_ctas(Ak.na, Ak.ntime, Ak.nchan), stream));
         done = true;
       }
     }
@@ -2472,7 +2553,7 @@ mb_status launch_tc_adjoint(const FusedArgs<float>& A, cudaStream_t stream) {
   // forward whose waits gave up does no work and keeps reporting it
   for (int k = 0, nsub = sub_count(A.na); k < nsub; ++k) {
     FusedArgs<float> Ak = sub_args(A, k, units);
-    if (Ak.npsrc > 0) MB_CHECK(run_tc_adj(Ak, units, stream));
+    if (Ak.npsrc > 0) MB_CHECK(run_tc_adj(Ak, tc_ctas(Ak.na, Ak.ntime, Ak.nchan), stream));
     if (Ak.nsrc > Ak.npsrc) {
       Ak.sbeg = Ak.npsrc;
       MB_CHECK(run_adj(Ak, true, units, stream));
@@ -2551,6 +2632,7 @@ mb_status batch_plan(mb_dtype dtype, const mb_dims* d, const mb_batch_set* sets,
   const size_t es = dtype == MB_FLOAT64 ? 8 : 4;
   const size_t nt = ext(d->ntime), na = ext(d->na), nbl = ext(d->nbl), nc = ext(d->nchan);
   const size_t units = nt * nc;
+  const size_t tc_units = size_t(tc_ctas(int(na), int(nt), int(nc)));  // CTAs of a tensor-core launch per set
   for (int i = 0; i < nsets; ++i) {
     const mb_batch_set& s = sets[i];
     const uint64_t n = uint64_t(s.npsrc) + s.ngsrc + s.nssrc;
@@ -2595,9 +2677,9 @@ mb_status batch_plan(mb_dtype dtype, const mb_dims* d, const mb_batch_set* sets,
       const int tile = tile_of_options(s.options);
       const bool tc = s.mode != MB_MODE_NATIVE;
       if (pass == 0) {
-        group_of(tc ? kBatchTcFwd : kBatchFwd, tc ? int(s.mode) : 0, tile).count += int(units);
+        group_of(tc ? kBatchTcFwd : kBatchFwd, tc ? int(s.mode) : 0, tile).count += int(tc ? tc_units : units);
       } else {
-        if (tc && s.npsrc > 0) group_of(kBatchTcAdj, 0, 0).count += int(units);
+        if (tc && s.npsrc > 0) group_of(kBatchTcAdj, 0, 0).count += int(tc_units);
         if (tc && s.ngsrc + s.nssrc > 0) group_of(kBatchExtAdj, 0, tile).count += int(units);
         if (!tc && nsrc_of(i) > 0) group_of(kBatchAdj, 0, tile).count += int(units);
       }
@@ -2652,6 +2734,7 @@ mb_status batch_prepare(const mb_dims* d, const mb_batch_set* sets, int nsets, v
                         cudaStream_t stream) {
   char* w = static_cast<char*>(ws);
   const int units = int(ext(d->ntime) * ext(d->nchan));
+  const int tc_units = tc_ctas(int(ext(d->na)), int(ext(d->ntime)), int(ext(d->nchan)));
   std::vector<BatchSet<T>> bs(nsets);
   for (int i = 0; i < nsets; ++i) {
     const mb_batch_set& s = sets[i];
@@ -2692,7 +2775,9 @@ mb_status batch_prepare(const mb_dims* d, const mb_batch_set* sets, int nsets, v
         case kBatchAdj: in = !tc && n > 0 && g.tile == tile; break;
       }
       if (!in) continue;
-      for (int u = 0; u < units; ++u) items[k++] = make_int2(i, u);
+      // the tensor-core kernels' CTAs may cover two channels each
+      const int nu = (g.kind == kBatchTcFwd || g.kind == kBatchTcAdj) ? tc_units : units;
+      for (int u = 0; u < nu; ++u) items[k++] = make_int2(i, u);
     }
     if (k != g.first + size_t(g.count)) return fail(MB_ERR_INVALID_ARG, "batch plan: item count mismatch");
   }
