@@ -1597,9 +1597,14 @@ constexpr int kTaPark = 6;            // float4 of parked state per item
 // Im (gB01 - gB10).
 constexpr int kTaAcc = 6;
 static_assert(kTaAcc <= 8, "per-source sums fit the 8-value reduce-scatter");
-using TaGeom = StageGeometry<kTaRowBytes>;
-using TaLayout = StageLayout<MB_MODE_SPLIT_BF16, kTaRowBytes>;
-constexpr size_t kJopBytes = 2 * size_t(2 * 8 * kTaRowBytes);       // hi + lo, 16 rows
+// The J operand (16 hi rows, then 16 lo rows) with K-adjacent core matrices
+// 144 bytes apart and 8-row groups 4672 bytes apart: a worker lane (a, i)
+// stores 4 bytes at K = 2a of row 2 (4 i + u), so a warp's 32 stores fall on
+// 32 distinct banks (dense 128 / 4096 put them on 4: an 8-way conflict).
+constexpr int kTaLBO = 144, kTaSBO = 32 * kTaLBO + 64;
+using TaGeom = StageGeometry<kTaRowBytes, kTaLBO, kTaSBO>;
+using TaLayout = StageLayout<MB_MODE_SPLIT_BF16, kTaRowBytes, kTaLBO, kTaSBO>;
+constexpr size_t kJopBytes = 4 * size_t(kTaSBO);  // hi + lo, 16 rows each
 constexpr int kTaParkBytes = int(sizeof(float4)) * kTaGroups * kTaItems * kTaPark * 128;
 // Bytes per row of Y (na Jones + 32) while it is formed in the park region.
 constexpr int kTaYRowBytes = 64 * int(sizeof(Jones<float>)) + 32;

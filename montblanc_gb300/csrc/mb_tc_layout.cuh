@@ -14,15 +14,20 @@
 
 namespace mb {
 
-template <int MODE, int ROWB = 128> struct StageLayout;
+// LBO and SBO may be padded beyond the dense 128 and (ROWB / 16) * 128 bytes
+// (multiples of 16 bytes), which moves K-adjacent core matrices and 8-row
+// groups onto other shared-memory banks.
+template <int MODE, int ROWB = 128, int LBO = 128, int SBO = (ROWB / 16) * 128> struct StageLayout;
 
-template <int ROWB>
+template <int ROWB, int LBO = 128, int SBO = (ROWB / 16) * 128>
 struct StageGeometry {
   static_assert(ROWB % 32 == 0, "a stage row holds whole MMA k-steps");
+  static_assert(LBO % 16 == 0 && LBO >= 128, "core matrices of 8 rows x 16 bytes");
+  static_assert(SBO % 16 == 0 && SBO >= (ROWB / 16) * LBO, "8-row groups must not overlap");
   static constexpr int kRowBytes = ROWB;
-  static constexpr int kMatBytes = 128 * kRowBytes;
-  static constexpr uint32_t kLBO = 128, kSBO = (ROWB / 16) * 128;
-  static constexpr int kKStepBytes = 256;
+  static constexpr int kMatBytes = 16 * SBO;  // 128 rows
+  static constexpr uint32_t kLBO = LBO, kSBO = SBO;
+  static constexpr int kKStepBytes = 2 * LBO;  // one MMA k-step: 2 core matrices along K
   static constexpr int kKSteps = kRowBytes / 32;
   __device__ __forceinline__ static uint32_t offset(int row, int kbyte) {
     return uint32_t((row >> 3) * kSBO + (kbyte >> 4) * kLBO + (row & 7) * 16 + (kbyte & 15));
@@ -30,8 +35,9 @@ struct StageGeometry {
   __device__ __forceinline__ static uint64_t desc(uint32_t saddr) { return tc::smem_desc(saddr, kLBO, kSBO); }
 };
 
-template <int ROWB> struct StageLayout<MB_MODE_SPLIT_TF32, ROWB> : StageGeometry<ROWB> {
-  using G = StageGeometry<ROWB>;
+template <int ROWB, int LBO, int SBO>
+struct StageLayout<MB_MODE_SPLIT_TF32, ROWB, LBO, SBO> : StageGeometry<ROWB, LBO, SBO> {
+  using G = StageGeometry<ROWB, LBO, SBO>;
   static constexpr int kElem = 4;
   static constexpr int kKT = ROWB / kElem;  // values of K per stage
   __host__ __device__ static constexpr uint32_t instr(uint32_t M, uint32_t N) { return tc::instr_desc(2, M, N); }
@@ -57,8 +63,9 @@ template <int ROWB> struct StageLayout<MB_MODE_SPLIT_TF32, ROWB> : StageGeometry
   }
 };
 
-template <int ROWB> struct StageLayout<MB_MODE_SPLIT_BF16, ROWB> : StageGeometry<ROWB> {
-  using G = StageGeometry<ROWB>;
+template <int ROWB, int LBO, int SBO>
+struct StageLayout<MB_MODE_SPLIT_BF16, ROWB, LBO, SBO> : StageGeometry<ROWB, LBO, SBO> {
+  using G = StageGeometry<ROWB, LBO, SBO>;
   static constexpr int kElem = 2;
   static constexpr int kKT = ROWB / kElem;  // values of K per stage
   __host__ __device__ static constexpr uint32_t instr(uint32_t M, uint32_t N) { return tc::instr_desc(1, M, N); }
