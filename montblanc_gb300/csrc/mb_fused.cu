@@ -44,7 +44,7 @@ __global__ void sum_partials_kernel(const double* __restrict__ partial, int n, d
 namespace {
 
 template <typename T> struct FwdTile;
-template <> struct FwdTile<float> { static constexpr int RP = 2, RQ = 4, ST = 16; };
+template <> struct FwdTile<float> { static constexpr int RP = 2, RQ = 4, ST = 32; };
 template <> struct FwdTile<double> { static constexpr int RP = 1, RQ = 2, ST = 8; };
 template <typename T> struct AdjTile;
 // FULL_Y: the Hermitian matrix Y of d chi^2 / dV is kept complete (na x na
@@ -78,6 +78,12 @@ int count_pair_tiles(int na, int RP, int RQ) {
   int npt = (na + RP - 1) / RP, nqt = (na + RQ - 1) / RQ, n = 0;
   for (int ip = 0; ip < npt; ++ip) n += nqt - (ip * RP) / RQ;
   return n;
+}
+
+// Bytes of npairs pair accumulators, dense or padded by 16 bytes after
+// every 4 pairs (pair_acc).
+inline size_t pair_acc_bytes(size_t jones_bytes, int npairs, bool pad) {
+  return jones_bytes * size_t(npairs) + (pad ? size_t(npairs / 4 + 1) * 16 : 0);
 }
 
 // with_J = false leaves out the Jones tile (a caller that places it itself),
@@ -124,9 +130,9 @@ SmemPlan make_plan_tile(int na, bool adjoint, bool with_J, int tile, bool with_g
   S.off_J = take(with_J ? size_t(S.jrow) * S.st : 0);
   S.off_gJ = take(adjoint && with_gJ ? size_t(S.jrow) * S.st : 0);
   S.off_V = take(adjoint && AdjTile<T>::FULL_Y ? sizeof(T) * size_t(na) * y_row_vals<T>(na)
-                                                : sizeof(Jones<T>) * size_t(S.npairs));
+                                                : pair_acc_bytes(sizeof(Jones<T>), S.npairs, !adjoint));
   // FP32 forward: low parts of float-float pair accumulators
-  S.off_Vlo = take(!adjoint && sizeof(T) == 4 ? sizeof(Jones<T>) * S.npairs : 0);
+  S.off_Vlo = take(!adjoint && sizeof(T) == 4 ? pair_acc_bytes(sizeof(Jones<T>), S.npairs, true) : 0);
   S.off_items = take(adjoint ? 0 : sizeof(int) * (S.nitems + 128));
   S.off_acc = take(adjoint ? sizeof(T) * S.st * kNAcc : 0);
   S.off_red = take(sizeof(double) * 32);
@@ -368,10 +374,27 @@ __device__ __forceinline__ void warp_keyed_add_stride(T* acc, int stride, int ke
   }
 }
 
+// Pair accumulator of packed pair index idx.  The CUDA-core forward (PAD)
+// leaves 16 bytes after every 4 pairs: the lanes of a warp fold the pair
+// tiles of one row, 4 pairs apart, which would otherwise sit a multiple of
+// 128 bytes apart, on the same banks (one 16-byte access per lane and
+// step: an 8-way conflict); with the pad they fall on 8 distinct 16-byte
+// bank groups.  The tensor-core forward's drain writes the dense layout.
+template <bool PAD, typename T>
+__device__ __forceinline__ Jones<T>* pair_acc(Jones<T>* base, int idx) {
+  if (!PAD) return base + idx;
+  return reinterpret_cast<Jones<T>*>(reinterpret_cast<unsigned char*>(base) + size_t(idx) * sizeof(Jones<T>) +
+                                     size_t(idx >> 2) * 16);
+}
+template <bool PAD, typename T>
+__device__ __forceinline__ const Jones<T>* pair_acc(const Jones<T>* base, int idx) {
+  return pair_acc<PAD>(const_cast<Jones<T>*>(base), idx);
+}
+
 // ---------------------------------------------------------------------------
 // Epilogue (shared with the tensor-core path)
 // ---------------------------------------------------------------------------
-template <typename T>
+template <bool PAD, typename T>
 __device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const Jones<T>* sV, Jones<T>* scratch,
                          double* red) {
   Jones<T>* sG = scratch;
@@ -409,7 +432,8 @@ __device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const J
         part += double(nan);
         if (A.want_grad) jstore(A.gV + 8 * ((size_t(t) * A.nbl + bl) * A.nchan + ch), jzero<T>());
       } else {
-        Jones<T> V = p <= q ? sV[pair_index(p, q, A.na)] : jherm(sV[pair_index(q, p, A.na)]);
+        Jones<T> V = p <= q ? *pair_acc<PAD>(sV, pair_index(p, q, A.na))
+                            : jherm(*pair_acc<PAD>(sV, pair_index(q, p, A.na)));
         if (A.accumulate_in) V = jadd(V, jload<T>(A.model_vis + 8 * vidx));
         if (A.partial_out) {
           jstore(A.model_vis + 8 * vidx, V);
@@ -481,15 +505,15 @@ __device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const J
 // FP32 mode, so that the sum over thousands of source tiles does not lose
 // the precision of FP32 (the per-tile partial sums are plain FP32).
 template <typename T>
-__device__ __forceinline__ void fold_pair(Jones<T>* sV, Jones<T>* sVlo, int idx, const Jones<T>& x) {
-  T* hi = reinterpret_cast<T*>(sV + idx);
+__device__ __forceinline__ void fold_pair(Jones<T>* sV, Jones<T>* sVlo, const Jones<T>& x) {
+  T* hi = reinterpret_cast<T*>(sV);
   const T* xv = reinterpret_cast<const T*>(&x);
   if (sVlo == nullptr) {
 #pragma unroll
     for (int k = 0; k < 8; ++k) hi[k] += xv[k];
     return;
   }
-  T* lo = reinterpret_cast<T*>(sVlo + idx);
+  T* lo = reinterpret_cast<T*>(sVlo);
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     T a = hi[k], b = xv[k];
@@ -505,7 +529,7 @@ __device__ __forceinline__ void fold_pair(Jones<T>* sV, Jones<T>* sVlo, int idx,
 // pair tile (k mod nitems) for the sources si = g, g + G, ... of the tile,
 // g = k / nitems, G = S.groups.  With G > 1 every thread owns at most one
 // item and the groups fold their partial sums one after the other.
-template <typename T, int RP, int RQ>
+template <typename T, int RP, int RQ, bool PAD>
 __device__ void consume_pairs(const FusedArgs<T>& A, const SmemPlan& S, int ns, const SrcInfo<T>* ss,
                               const AntInfo<T>* sa, const Jones<T>* sJ, Jones<T>* sV, Jones<T>* sVlo,
                               const int* items, bool extended, T kg, T ks) {
@@ -562,7 +586,10 @@ __device__ void consume_pairs(const FusedArgs<T>& A, const SmemPlan& S, int ns, 
 #pragma unroll
           for (int c = 0; c < RQ; ++c) {
             int p = p0 + r, q = q0 + c;
-            if (p <= q && q < A.na) fold_pair(sV, sVlo, pair_index(p, q, A.na), acc[r][c]);
+            if (p <= q && q < A.na) {
+              const int idx = pair_index(p, q, A.na);
+              fold_pair(pair_acc<PAD>(sV, idx), sVlo ? pair_acc<PAD>(sVlo, idx) : nullptr, acc[r][c]);
+            }
           }
       }
     }
@@ -589,8 +616,8 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A_
   const int t = unit / A.nchan, ch = unit - t * A.nchan;
   load_antennas(A, t, ch, sa);
   for (int i = threadIdx.x; i < S.npairs; i += blockDim.x) {
-    sV[i] = jzero<T>();
-    if (sVlo) sVlo[i] = jzero<T>();
+    *pair_acc<true>(sV, i) = jzero<T>();
+    if (sVlo) *pair_acc<true>(sVlo, i) = jzero<T>();
   }
   if (threadIdx.x == 0) {
     const int npt = (A.na + RP - 1) / RP, nqt = (A.na + RQ - 1) / RQ;
@@ -610,15 +637,16 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A_
     __syncthreads();
     produce_jones(A, S, t, ch, s0, ns, ss, sa, sJ, cp);
     __syncthreads();
-    consume_pairs<T, RP, RQ>(A, S, ns, ss, sa, sJ, sV, sVlo, items, s0 >= A.npsrc, kg, ks);
+    consume_pairs<T, RP, RQ, true>(A, S, ns, ss, sa, sJ, sV, sVlo, items, s0 >= A.npsrc, kg, ks);
     __syncthreads();
     s0 = s1;
   }
   if (sVlo) {  // collapse the float-float accumulators
-    for (int i = threadIdx.x; i < S.npairs; i += blockDim.x) sV[i] = jadd(sV[i], sVlo[i]);
+    for (int i = threadIdx.x; i < S.npairs; i += blockDim.x)
+      *pair_acc<true>(sV, i) = jadd(*pair_acc<true>(sV, i), *pair_acc<true>(sVlo, i));
     __syncthreads();
   }
-  epilogue(A, t, ch, unit, sV, sJ, red);
+  epilogue<true>(A, t, ch, unit, sV, sJ, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -1081,13 +1109,13 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
       __syncthreads();
       produce_jones(A, S, t, ch + c, s0, ns, ss, sac, sJ, cp[c]);
       __syncthreads();
-      consume_pairs<float, 2, 4>(A, S, ns, ss, sac, sJ, sVc, sVlo, items, true, kg, ks);
+      consume_pairs<float, 2, 4, false>(A, S, ns, ss, sac, sJ, sVc, sVlo, items, true, kg, ks);
       __syncthreads();
       s0 = s1;
     }
     for (int i = tid; i < S.npairs; i += blockDim.x) sVc[i] = jadd(sVc[i], sVlo[i]);
     __syncthreads();
-    epilogue(A, t, ch + c, unit + c, sVc, sJ, red);
+    epilogue<false>(A, t, ch + c, unit + c, sVc, sJ, red);
     __syncthreads();
     if (aborted && tid == 0) {
       A.partial[unit + c] = double(NAN);
