@@ -87,3 +87,37 @@ def test_sub_arrays_launch_per_block_pair():
         prob.forward(mode='split_tf32')
         torch.cuda.synchronize()
     assert kt.times()['coh_tc_fwd_kernel'][1] == 6
+
+
+@pytest.mark.parametrize('dtype', ['double', 'float'])
+def test_sub_arrays_with_source_batches(dtype):
+    """The reference's source batches (nsrc extents, partial sums carried in
+    model_vis) on a 75-antenna array split into sub-arrays: 12 point sources,
+    then 4 point, 4 gaussian and 4 sersic sources, against the reference's
+    one-pass result."""
+    import ctypes
+    import torch
+    from montblanc_gb300 import _cabi
+    from montblanc_gb300.rime import RimeProblem
+    P, ref = golden_io.load('wide_na75')
+    assert (P['npsrc'], P['ngsrc'], P['nssrc']) == (16, 4, 4)
+    prob = RimeProblem.from_numpy(P, dtype=dtype)
+    vis, chi2 = prob.empty_vis(), prob.empty_chi2()
+    x2 = torch.zeros(1, dtype=torch.float64, device='cuda')
+    ws = prob.workspace('native', False)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for lo, hi, ext in ((0, 12, {'npsrc': (0, 12), 'ngsrc': (0, 0), 'nssrc': (0, 0)}),
+                        (12, 24, {'npsrc': (0, 4), 'ngsrc': (0, 4), 'nssrc': (0, 4)})):
+        sl = slice(lo, hi)
+        ov = {'lm': prob.arrays['lm'][sl].contiguous(), 'stokes': prob.arrays['stokes'][sl].contiguous(),
+              'alpha': prob.arrays['alpha'][sl].contiguous()}
+        e = dict(ext)
+        e['nsrc'] = (lo, hi)
+        d = _cabi.make_dims(prob.ntime, prob.na, prob.nbl, prob.nchan, 16, 4, 4, beam=prob.beam,
+                            extents=e, globals_={'nsrc': 24})
+        inp = prob.inputs(**ov)
+        _cabi.call('mb_rime_forward', prob.mb_dtype, 0, ctypes.byref(d), ctypes.byref(prob.mb_props()),
+                   prob.options(), ctypes.byref(inp), vis.data_ptr(), chi2.data_ptr(), x2.data_ptr(), 0,
+                   ws.data_ptr(), ws.numel(), stream)
+    assert golden_io.rel_err(vis.cpu().numpy(), ref['vis_out']) < TOL[dtype]['vis']
+    assert abs(x2.item() - ref['X2']) <= TOL[dtype]['X2'] * abs(ref['X2'])
