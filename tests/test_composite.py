@@ -180,28 +180,31 @@ def test_streaming_gradient_matches_whole_problem():
 
 
 @pytest.mark.gpu
-def test_streaming_matches_reference_fixture():
+@pytest.mark.parametrize('name, chunk, nbatch', [('units_medium_mixed', (2, 2), 5), ('wide_na75', (2, 1), 1)])
+def test_streaming_matches_reference_fixture(name, chunk, nbatch):
     """The streamed solve of 3 time steps x 3 channels of the 100 x 27 x 64
     workload (all 1250 sources, tests/golden/units_medium_mixed, outputs of
     the reference's CPUSolver) in (2, 2) visibility chunks and 300-source
-    batches: model visibilities, chi^2 terms and chi^2 against the
-    reference, the streamed gradient against the FP64 oracle's."""
+    batches, and the 75-antenna array of tests/golden/wide_na75 (weights,
+    flags; antenna sub-arrays inside each chunk): model visibilities,
+    chi^2 terms and chi^2 against the reference, the streamed gradient
+    against the FP64 oracle's."""
     import golden_io
     import montblanc_gb300 as mb
-    P, ref = golden_io.load('units_medium_mixed')
+    P, ref = golden_io.load(name)
     ntime, na = P['uvw'].shape[:2]
     lw, mh, nud = P['E_beam'].shape[:3]
     supplied = {n: P[n] for n in ARRAYS}
     cfg = mb.rime_solver_cfg(na=na, ntime=ntime, nchan=P['frequency'].shape[0], nbl=P['antenna1'].shape[1],
                              sources=mb.sources(point=P['npsrc'], gaussian=P['ngsrc'], sersic=P['nssrc']),
                              beam_lw=lw, beam_mh=mh, beam_nud=nud, dtype='double', version='v5',
-                             data_source='empty', vis_chunk=(2, 2), source_batch_size=300, nsolvers=2,
-                             array_cfg={'supplied': supplied})
+                             data_source='empty', vis_chunk=chunk, source_batch_size=300, nsolvers=2,
+                             weight_vector=bool(P['use_weight_vector']), array_cfg={'supplied': supplied})
     s = mb.rime_solver(cfg)
     for n in ('gauss_scale', 'two_pi_over_c', 'sigma_sqrd', 'beam_ll', 'beam_lm', 'beam_lfreq', 'beam_ul',
               'beam_um', 'beam_ufreq'):
         getattr(s, 'set_' + n)(P[n])
-    assert len(s.vis_chunks()) == 4 and len(s.source_batches()) == 5
+    assert len(s.vis_chunks()) == 4 and len(s.source_batches()) == nbatch
     s.solve()
     assert golden_io.rel_err(s.model_vis, ref['vis_out']) < 1e-10
     assert abs(s.X2 - ref['X2']) <= 1e-10 * abs(ref['X2'])
