@@ -48,13 +48,15 @@ NCU_LIMITER = {
     'coh_tc_adj_kernel': {
         'source': 'profiles/coh_tc_adj_kernel_profile_point.md',
         'limiter': 'CUDA-core issue and latency of the per-(source, antenna) producer and chain',
-        'sm__pipe_tensor_cycles_active': 0.103, 'smsp__issue_active': 0.421,
-        'pipe_fma': 0.220, 'pipe_alu': 0.262, 'pipe_fp64': 0.058, 'pipe_xu': 0.044},
+        'sm__pipe_tensor_cycles_active': 0.101, 'smsp__issue_active': 0.425,
+        'pipe_fma': 0.212, 'pipe_alu': 0.265, 'pipe_fp64': 0.058, 'pipe_xu': 0.045,
+        'thread_instructions_per_item': 792},
     'coh_tc_fwd_kernel': {
         'source': 'profiles/coh_tc_fwd_kernel_profile_point.md',
         'limiter': 'CUDA-core issue and latency of the per-(source, antenna) producer; TMEM drains',
-        'sm__pipe_tensor_cycles_active': 0.302, 'smsp__issue_active': 0.452,
-        'pipe_fma': 0.184, 'pipe_alu': 0.352, 'pipe_fp64': 0.074, 'pipe_xu': 0.041},
+        'sm__pipe_tensor_cycles_active': 0.295, 'smsp__issue_active': 0.453,
+        'pipe_fma': 0.167, 'pipe_alu': 0.354, 'pipe_fp64': 0.073, 'pipe_xu': 0.040,
+        'thread_instructions_per_item': 634},
 }
 
 # DRAM bytes per launch from a one-kernel ncu capture on the profile_point
