@@ -128,3 +128,44 @@ def test_source_tile_options():
         st = _cabi.lib.mb_rime_forward(_cabi.MB_FLOAT32, 0, ctypes.byref(d), ctypes.byref(p), opts,
                                        ctypes.byref(inp), None, None, x2, 0, fake, n - 1, None)
         assert _cabi.STATUS_NAMES[st] == want, (opts, _cabi.STATUS_NAMES[st])
+
+
+def test_batch_plan_validation():
+    """mb_rime_batch_workspace_size (host-side planning, no launch): a valid
+    batch of sets has a workspace that grows with its sets; arrays above 64
+    antennas, split modes on FP64 data, non-tile option bits and sets
+    without source arrays are refused with 0 and a message."""
+    from montblanc_gb300 import _cabi
+    lib = _cabi.lib
+    dummy = ctypes.c_void_p(0x1000)
+
+    def sets(specs):
+        arr = (_cabi.MbBatchSet * max(len(specs), 1))()
+        for i, (npt, ng, ns, mode, opts) in enumerate(specs):
+            b = arr[i]
+            b.npsrc, b.ngsrc, b.nssrc, b.mode, b.options, b.reserved = npt, ng, ns, mode, opts, 0
+            b.lm = b.stokes = b.alpha = dummy
+            b.gauss_shape = dummy if ng else None
+            b.sersic_shape = dummy if ns else None
+        return arr, len(specs)
+
+    def size(na, specs, dtype=_cabi.MB_FLOAT32):
+        d = _cabi.make_dims(4, na, na * (na - 1) // 2, 3, 0, beam=(8, 8, 4))
+        arr, n = sets(specs)
+        return lib.mb_rime_batch_workspace_size(dtype, ctypes.byref(d), arr, n)
+
+    tc, nat = _cabi.MB_MODE_SPLIT_TF32, _cabi.MB_MODE_NATIVE
+    one = size(27, [(10, 2, 1, tc, 0)])
+    two = size(27, [(10, 2, 1, tc, 0), (5, 0, 0, nat, _cabi.source_tile_bits(16))])
+    assert 0 < one < two
+    assert size(65, [(10, 0, 0, nat, 0)]) == 0
+    assert '64 antennas' in lib.mb_last_error_string().decode()
+    assert size(27, [(10, 0, 0, tc, 0)], dtype=_cabi.MB_FLOAT64) == 0
+    assert 'FLOAT32' in lib.mb_last_error_string().decode()
+    assert size(27, [(10, 0, 0, nat, _cabi.MB_APPLY_WEIGHTS)]) == 0
+    assert 'source-tile' in lib.mb_last_error_string().decode()
+    arr, n = sets([(10, 0, 0, nat, 0)])
+    arr[0].lm = None
+    d = _cabi.make_dims(4, 27, 351, 3, 0, beam=(8, 8, 4))
+    assert lib.mb_rime_batch_workspace_size(_cabi.MB_FLOAT32, ctypes.byref(d), arr, n) == 0
+    assert 'lm' in lib.mb_last_error_string().decode()
