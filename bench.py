@@ -542,6 +542,37 @@ def time_plain_slice(P, prob, ws, workload, clk, ntime=20, steps=3, warmup=1):
     return out
 
 
+def time_fp64_forward(P, prob, ws, ntime=1, steps=1, warmup=1):
+    """The reference's default configuration through the drop-in path: the
+    FP64 forward (model visibilities, chi^2 terms and chi^2, no gradient)
+    of the CUDA-core kernels on the first ``ntime`` time steps of the
+    workload, all channels, sources and baselines."""
+    import torch
+    from montblanc_gb300.rime import RimeProblem
+    nt = min(ntime, prob.ntime)
+    Q = subset_problem(P, prob, list(range(nt)), list(range(prob.nchan)))
+    sub = RimeProblem.from_numpy(Q, dtype='double')
+    vis, terms = sub.empty_vis(), sub.empty_chi2()
+    for _ in range(warmup):
+        sub.forward(mode='native', model_vis=vis, chi_sqrd_result=terms)
+    torch.cuda.synchronize()
+    barrier(ws)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        sub.forward(mode='native', model_vis=vis, chi_sqrd_result=terms)
+    e1.record()
+    e1.synchronize()
+    ms = max_over_ranks(ws, e0.elapsed_time(e1) / steps)
+    n = prob.nsrc * nt * prob.nbl * prob.nchan
+    del sub, vis, terms
+    torch.cuda.empty_cache()
+    return {'value': ws * n / (ms * 1e-3), 'unit': UNIT, 'ms_per_step': ms, 'steps': steps, 'warmup': warmup,
+            'what': 'FP64 forward (chi^2, model visibilities, chi^2 terms; no gradient), mode native, the '
+                    'drop-in rime_solver default', 'terms_per_step': n,
+            'sample': 'first %d of %d time steps, all sources, baselines and channels' % (nt, prob.ntime)}
+
+
 def time_e2e(prob, mode, steps, warmup, ws):
     """Through the public API with host buffers: every step copies its
     inputs from pinned host memory and reads chi^2 and all gradients back
@@ -686,11 +717,12 @@ def main():
     ms_max = max_over_ranks(ws, ms)
     value = whole_job_value(ws, terms, ms_max)
 
-    plain = None
+    plain = fp64_fwd = None
     if not args.no_plain and args.mode != 'native':
         # The plain FP32 CUDA-core form on the first 20 time steps of the same
         # workload (throughput per term does not depend on the time extent).
         plain = time_plain_slice(P, prob, ws, args.workload, clk)
+        fp64_fwd = time_fp64_forward(P, prob, ws)
     e2e = None
     if not args.no_e2e:
         ems, h2d, d2h, phases = time_e2e(prob, args.mode, args.steps, 1, ws)
@@ -718,6 +750,8 @@ def main():
         'gpu_launches': launches,
         'clocks': clk,
     }
+    if fp64_fwd:
+        line['fp64_forward'] = fp64_fwd
     if plain:
         line['plain_fp32'] = plain
         line['split_over_plain'] = value / plain['value']
