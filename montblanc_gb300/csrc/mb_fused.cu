@@ -313,15 +313,29 @@ __device__ __forceinline__ Jones<T> compute_jones(const FusedArgs<T>& A, int t, 
 }
 
 // J(s, a) for the tile into the Jones tile sJ; padded antennas get zeros.
-template <typename T>
+// DF (the FP64 forward): each FP64 value is stored as the double-float pair
+// (hi, lo) = (float(x), float(x - hi)) in the same 8 bytes, for the pair
+// sums of consume_pairs.
+template <typename T, bool DF = false>
 __device__ void produce_jones(const FusedArgs<T>& A, const SmemPlan& S, int t, int ch, int s0, int ns,
                               const SrcInfo<T>* ss, const AntInfo<T>* sa, Jones<T>* sJ, const ChanPos<T>& cp) {
   const T f = A.freq[ch];
   const double nu_over_c = double(f) / kLightSpeed;
   for (int i = threadIdx.x; i < ns * S.nap; i += blockDim.x) {
     int si = i / S.nap, a = i - si * S.nap;
-    *jtile(sJ, S, si, a) = a < A.na ? compute_jones(A, t, s0 + si, a, ss[si], sa[a], f, nu_over_c, cp, ch)
-                                    : jzero<T>();
+    const Jones<T> J = a < A.na ? compute_jones(A, t, s0 + si, a, ss[si], sa[a], f, nu_over_c, cp, ch)
+                                : jzero<T>();
+    if constexpr (DF && sizeof(T) == 8) {
+      const double* v = reinterpret_cast<const double*>(&J);
+      float2* o = reinterpret_cast<float2*>(jtile(sJ, S, si, a));
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const float h = float(v[k]);
+        o[k] = make_float2(h, float(v[k] - double(h)));
+      }
+    } else {
+      *jtile(sJ, S, si, a) = J;
+    }
   }
 }
 
@@ -525,6 +539,163 @@ __device__ __forceinline__ void fold_pair(Jones<T>* sV, Jones<T>* sVlo, const Jo
   }
 }
 
+// Double-float arithmetic for the FP64 forward's pair sums.  GB300 runs FP32
+// at 64 times its FP64 rate, so the O(na^2) pair sums of the FP64 forward
+// use values held as hi + lo FP32 pairs (about 48 significant bits): an
+// exact product by FMA (Dekker's product, with the cross terms of the low
+// parts) added to the accumulator by TwoSum (Knuth), 11 FP32 operations per
+// multiply-add against one FP64 FMA; per tile the sums are converted to
+// FP64 and folded into the FP64 pair accumulators.  The per-antenna terms
+// J and the shape factors are formed in FP64.
+struct Df {
+  float h, l;
+};
+struct CDf {
+  Df r, i;
+};
+struct JDf {
+  CDf a, b, c, d;
+};
+
+__device__ __forceinline__ Df df_of(double x) {
+  const float h = float(x);
+  return {h, float(x - double(h))};
+}
+__device__ __forceinline__ double df_value(Df x) { return double(x.h) + double(x.l); }
+
+// acc += a * b
+__device__ __forceinline__ void df_mac(Df& acc, Df a, Df b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float s = acc.h + p;
+  const float v = s - acc.h;
+  const float t = (acc.h - (s - v)) + (p - v);
+  acc.h = s;
+  acc.l += t + e;
+}
+__device__ __forceinline__ Df df_neg(Df a) { return {-a.h, -a.l}; }
+// a * b rounded back to a double-float (the product's low part kept)
+__device__ __forceinline__ Df df_mul(Df a, Df b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float s = p + e;
+  return {s, e - (s - p)};
+}
+// acc += a * conj(b)
+__device__ __forceinline__ void cmacc_df(CDf& acc, const CDf& a, const CDf& b) {
+  df_mac(acc.r, a.r, b.r);
+  df_mac(acc.r, a.i, b.i);
+  df_mac(acc.i, a.i, b.r);
+  df_mac(acc.i, df_neg(a.r), b.i);
+}
+// acc += X * Y^H
+__device__ __forceinline__ void jmac_h_df(JDf& acc, const JDf& X, const JDf& Y) {
+  cmacc_df(acc.a, X.a, Y.a); cmacc_df(acc.a, X.b, Y.b);
+  cmacc_df(acc.b, X.a, Y.c); cmacc_df(acc.b, X.b, Y.d);
+  cmacc_df(acc.c, X.c, Y.a); cmacc_df(acc.c, X.d, Y.b);
+  cmacc_df(acc.d, X.c, Y.c); cmacc_df(acc.d, X.d, Y.d);
+}
+// A Jones tile entry written by produce_jones<double, true>.
+__device__ __forceinline__ JDf jdf_load(const Jones<double>* p) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  const float4 x0 = q[0], x1 = q[1], x2 = q[2], x3 = q[3];
+  JDf J;
+  J.a.r = {x0.x, x0.y}; J.a.i = {x0.z, x0.w};
+  J.b.r = {x1.x, x1.y}; J.b.i = {x1.z, x1.w};
+  J.c.r = {x2.x, x2.y}; J.c.i = {x2.z, x2.w};
+  J.d.r = {x3.x, x3.y}; J.d.i = {x3.z, x3.w};
+  return J;
+}
+__device__ __forceinline__ JDf jdf_zero() {
+  JDf J;
+  J.a.r = J.a.i = J.b.r = J.b.i = J.c.r = J.c.i = J.d.r = J.d.i = Df{0.f, 0.f};
+  return J;
+}
+__device__ __forceinline__ JDf jdf_scale(const JDf& X, Df s) {
+  JDf R;
+  R.a.r = df_mul(X.a.r, s); R.a.i = df_mul(X.a.i, s);
+  R.b.r = df_mul(X.b.r, s); R.b.i = df_mul(X.b.i, s);
+  R.c.r = df_mul(X.c.r, s); R.c.i = df_mul(X.c.i, s);
+  R.d.r = df_mul(X.d.r, s); R.d.i = df_mul(X.d.i, s);
+  return R;
+}
+__device__ __forceinline__ Jones<double> jdf_value(const JDf& X) {
+  return {{df_value(X.a.r), df_value(X.a.i)}, {df_value(X.b.r), df_value(X.b.i)},
+          {df_value(X.c.r), df_value(X.c.i)}, {df_value(X.d.r), df_value(X.d.i)}};
+}
+
+// consume_pairs for the FP64 forward on double-float Jones tiles (same work
+// items, groups and fold as consume_pairs).
+template <int RP, int RQ, bool PAD>
+__device__ void consume_pairs_df(const FusedArgs<double>& A, const SmemPlan& S, int ns, const SrcInfo<double>* ss,
+                                 const AntInfo<double>* sa, const Jones<double>* sJ, Jones<double>* sV,
+                                 const int* items, bool extended, double kg, double ks) {
+  const int total = S.nitems * S.groups;
+  const int rounds = (total + blockDim.x - 1) / blockDim.x;
+  for (int round = 0; round < rounds; ++round) {
+    const int k = round * blockDim.x + threadIdx.x;
+    const bool active = k < total;
+    const int item = active ? k % S.nitems : 0, g = active ? k / S.nitems : 0;
+    const int it = items[item];
+    const int p0 = (it & 0xffff) * RP, q0 = (it >> 16) * RQ;
+    JDf acc[RP][RQ];
+    double u[RP][RQ], v[RP][RQ];
+#pragma unroll
+    for (int r = 0; r < RP; ++r)
+#pragma unroll
+      for (int c = 0; c < RQ; ++c) {
+        acc[r][c] = jdf_zero();
+        if (extended) {
+          int pp = min(p0 + r, A.na - 1), qq = min(q0 + c, A.na - 1);
+          u[r][c] = sa[qq].u - sa[pp].u;
+          v[r][c] = sa[qq].v - sa[pp].v;
+        }
+      }
+    if (active) {
+      for (int si = g; si < ns; si += S.groups) {
+        JDf Ja[RP], Jb[RQ];
+#pragma unroll
+        for (int r = 0; r < RP; ++r) Ja[r] = jdf_load(jtile(sJ, S, si, p0 + r));
+#pragma unroll
+        for (int c = 0; c < RQ; ++c) Jb[c] = jdf_load(jtile(sJ, S, si, q0 + c));
+        if (!extended) {
+#pragma unroll
+          for (int r = 0; r < RP; ++r)
+#pragma unroll
+            for (int c = 0; c < RQ; ++c) jmac_h_df(acc[r][c], Ja[r], Jb[c]);
+        } else {
+          const SrcInfo<double>& src = ss[si];
+#pragma unroll
+          for (int r = 0; r < RP; ++r)
+#pragma unroll
+            for (int c = 0; c < RQ; ++c) {
+              const double sh = shape_factor<double>(src.type, u[r][c], v[r][c], src.s0, src.s1, src.s2, kg, ks);
+              jmac_h_df(acc[r][c], jdf_scale(Ja[r], df_of(sh)), Jb[c]);
+            }
+        }
+      }
+    }
+    for (int gg = 0; gg < S.groups; ++gg) {
+      if (S.groups > 1) __syncthreads();
+      if (active && g == gg) {
+#pragma unroll
+        for (int r = 0; r < RP; ++r)
+#pragma unroll
+          for (int c = 0; c < RQ; ++c) {
+            int p = p0 + r, q = q0 + c;
+            if (p <= q && q < A.na)
+              fold_pair(pair_acc<PAD>(sV, pair_index(p, q, A.na)), static_cast<Jones<double>*>(nullptr),
+                        jdf_value(acc[r][c]));
+          }
+      }
+    }
+  }
+}
+
 // Accumulate the tile's sources into the pair matrix.  Work item k covers
 // pair tile (k mod nitems) for the sources si = g, g + G, ... of the tile,
 // g = k / nitems, G = S.groups.  With G > 1 every thread owns at most one
@@ -635,9 +806,15 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A_
     int ns = s1 - s0;
     load_sources(A, t, ch, s0, ns, ss);
     __syncthreads();
-    produce_jones(A, S, t, ch, s0, ns, ss, sa, sJ, cp);
-    __syncthreads();
-    consume_pairs<T, RP, RQ, true>(A, S, ns, ss, sa, sJ, sV, sVlo, items, s0 >= A.npsrc, kg, ks);
+    if constexpr (sizeof(T) == 8) {  // FP64: pair sums in double-float
+      produce_jones<T, true>(A, S, t, ch, s0, ns, ss, sa, sJ, cp);
+      __syncthreads();
+      consume_pairs_df<RP, RQ, true>(A, S, ns, ss, sa, sJ, sV, items, s0 >= A.npsrc, kg, ks);
+    } else {
+      produce_jones(A, S, t, ch, s0, ns, ss, sa, sJ, cp);
+      __syncthreads();
+      consume_pairs<T, RP, RQ, true>(A, S, ns, ss, sa, sJ, sV, sVlo, items, s0 >= A.npsrc, kg, ks);
+    }
     __syncthreads();
     s0 = s1;
   }
