@@ -121,3 +121,42 @@ def test_sub_arrays_with_source_batches(dtype):
                    ws.data_ptr(), ws.numel(), stream)
     assert golden_io.rel_err(vis.cpu().numpy(), ref['vis_out']) < TOL[dtype]['vis']
     assert abs(x2.item() - ref['X2']) <= TOL[dtype]['X2'] * abs(ref['X2'])
+
+
+@pytest.mark.parametrize('na', [32, 33, 65])
+def test_antenna_count_edges(na):
+    """The edges of the kernels' antenna layouts against the FP64 oracle:
+    32 antennas (two channels per tensor-core CTA, exactly full), 33 (one
+    channel per CTA), 65 (three sub-arrays, the last block one antenna);
+    FP64 forward and adjoint, the TF32 split forward."""
+    from montblanc_gb300 import synth
+    from montblanc_gb300.rime import RimeProblem
+    from oracle import adjoint as OA
+    from oracle import rime_v4 as O
+    P = synth.make_problem(ntime=2, na=na, nchan=3, npsrc=9, ngsrc=2, nssrc=1, seed=na, beam_shape=(12, 12, 6),
+                           flag_fraction=0.05)
+    model, _, _ = O.forward(P)
+    synth.add_noise(P, model, sigma=0.1, seed=na + 1)
+    # inputs representable in FP32, so that the FP32 run and the oracle see
+    # the same values (the phase of a rounded uvw differs by ~1e-4 rad)
+    for k, v in P.items():
+        if isinstance(v, np.ndarray) and v.dtype == np.float64:
+            P[k] = v.astype(np.float32).astype(np.float64)
+        elif isinstance(v, np.ndarray) and v.dtype == np.complex128:
+            P[k] = v.astype(np.complex64).astype(np.complex128)
+    ref_vis, _, ref_x2 = O.forward(P)
+    ref_x2g, ref_g = OA.chi2_grad(P)
+    prob = RimeProblem.from_numpy(P, dtype='double')
+    vis = prob.empty_vis()
+    x2 = prob.forward(model_vis=vis, want_grad=True).item()
+    g = {k: v.cpu().numpy() for k, v in prob.adjoint().items()}
+    assert golden_io.rel_err(vis.cpu().numpy(), ref_vis) < 1e-10
+    assert abs(x2 - ref_x2) <= 1e-10 * abs(ref_x2)
+    for k, r in ref_g.items():
+        if r.size:
+            assert norm_err(g[k], r) < 1e-9, (k, norm_err(g[k], r))
+    p32 = RimeProblem.from_numpy(P, dtype='float')
+    v32 = p32.empty_vis()
+    x2s = p32.forward(mode='split_tf32', model_vis=v32).item()
+    assert norm_err(v32.cpu().numpy(), ref_vis) < VIS_BOUND['split_tf32']
+    assert abs(x2s - ref_x2) <= X2_BOUND['split_tf32'] * abs(ref_x2)
