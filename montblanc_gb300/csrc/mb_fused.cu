@@ -172,6 +172,13 @@ __device__ __forceinline__ void use_set(FusedArgs<T>& A, const BatchSet<T>& b) {
   A.acc_lm = b.acc_lm; A.acc_stokes = b.acc_stokes; A.acc_alpha = b.acc_alpha;
   A.acc_gauss = b.acc_gauss; A.acc_sersic = b.acc_sersic;
   if (A.sbeg < 0) A.sbeg = b.npsrc;
+  // the split forms' extended-source sums: written by the CUDA-core launch
+  // (partial_out), added in by the tensor-core launch (accumulate_in)
+  if (A.partial_out) A.model_vis = b.vis_ext;
+  if (A.accumulate_in) {
+    A.vis_in = b.vis_ext;
+    A.accumulate_in = b.vis_ext != nullptr;
+  }
 }
 
 // The (time, channel) unit of this CTA: blockIdx.x for a single problem;
@@ -448,7 +455,7 @@ __device__ void epilogue(const FusedArgs<T>& A, int t, int ch, int unit, const J
       } else {
         Jones<T> V = p <= q ? *pair_acc<PAD>(sV, pair_index(p, q, A.na))
                             : jherm(*pair_acc<PAD>(sV, pair_index(q, p, A.na)));
-        if (A.accumulate_in) V = jadd(V, jload<T>(A.model_vis + 8 * vidx));
+        if (A.accumulate_in) V = jadd(V, jload<T>(A.vis_in + 8 * vidx));
         if (A.partial_out) {
           jstore(A.model_vis + 8 * vidx, V);
         } else {
@@ -801,7 +808,7 @@ __global__ void __launch_bounds__(kFwdMaxThreads) coh_fwd_kernel(FusedArgs<T> A_
   const T f = A.freq[ch];
   const ChanPos<T> cp = chan_pos<T>(f, A.lfreq, A.ufreq, A.nud);
   const T kg = A.gauss_scale * f, ks = A.two_pi_over_c * f;
-  for (int s0 = 0; s0 < A.nsrc;) {
+  for (int s0 = A.sbeg; s0 < A.nsrc;) {
     int s1 = s0 < A.npsrc ? min(s0 + S.st, A.npsrc) : min(s0 + S.st, A.nsrc);
     int ns = s1 - s0;
     load_sources(A, t, ch, s0, ns, ss);
@@ -1280,7 +1287,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
     }
     __syncthreads();
     const float kg = A.gauss_scale * fc[c], ks = A.two_pi_over_c * fc[c];
-    for (int s0 = A.npsrc; s0 < A.nsrc && !aborted;) {
+    for (int s0 = A.npsrc; s0 < A.nsrc && A.tc_ext && !aborted;) {
       const int s1 = min(s0 + S.st, A.nsrc), ns = s1 - s0;
       load_sources(A, t, ch + c, s0, ns, ss);
       __syncthreads();
@@ -2455,7 +2462,8 @@ FusedArgs<T> sub_args(const FusedArgs<T>& A, int k, int units) {
 }
 
 struct WsLayout {
-  size_t phi, plane, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, err, total;
+  size_t phi, plane, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, acc_end, err,
+      vis_ext, total;
 };
 
 WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_grad) {
@@ -2478,6 +2486,11 @@ WsLayout ws_layout(mb_dtype dtype, mb_mode mode, const mb_dims* d, bool want_gra
   L.acc_sersic = take(want_grad ? 3 * nx * 8 : 0);
   L.acc_end = o;
   L.err = take(sizeof(int));
+  // split forms: the extended sources' visibility sums (local strides, as
+  // the epilogue indexes visibilities)
+  L.vis_ext = take(mode != MB_MODE_NATIVE && dtype == MB_FLOAT32 && (ng + nx) > 0
+                       ? size_t(d->ntime.local_size) * d->nbl.local_size * d->nchan.local_size * 8 * es
+                       : 0);
   L.total = o;
   return L;
 }
@@ -2515,6 +2528,7 @@ mb_status fill_args(FusedArgs<T>& A, const mb_dims* d, const mb_props* P, uint32
   A.sersic = (const T*)in->sersic_shape; A.weight = (const T*)in->weight_vector; A.obs = (const T*)in->observed_vis;
   A.ant1 = in->antenna1; A.ant2 = in->antenna2; A.flag = in->flag;
   A.model_vis = (T*)model_vis; A.chi2 = (T*)chi2;
+  A.vis_in = (const T*)model_vis; A.tc_ext = true;
   A.err = nullptr;
   A.phi = nullptr; A.partial = nullptr; A.gV = nullptr; A.dG = nullptr;
   A.plane = nullptr; A.bsq0 = nullptr;
@@ -2737,12 +2751,33 @@ mb_status launch_forward(const FusedArgs<T>& A, mb_mode mode, double* X2, void* 
   // sub-arrays add their dchi^2/dG terms into it
   if (nsub > 1 && A.want_grad && A.dG)
     MB_CUDA(cudaMemsetAsync(A.dG, 0, size_t(A.ntime) * A.na * A.nchan * 8 * sizeof(T), stream));
+  // Split forms with extended sources: the CUDA-core forward sums the
+  // extended sources first (onto the caller's partial sums, if any) into
+  // the workspace's visibility region, and the tensor-core forward adds its
+  // point sources to those and finishes (G, flags, chi^2).  The CUDA-core
+  // kernel runs several CTAs per SM; inside the tensor-core CTA the same
+  // sums ran at a fraction of its speed.
+  const bool ext_first = mode != MB_MODE_NATIVE && A.nsrc > A.npsrc && L.vis_ext != L.total;
+  T* vis_ext = reinterpret_cast<T*>(static_cast<char*>(ws) + L.vis_ext);
   for (int k = 0; k < nsub; ++k) {
     const FusedArgs<T> Ak = sub_args(A, k, units);
     bool done = false;
     if constexpr (sizeof(T) == 4) {
       if (mode != MB_MODE_NATIVE) {
-        MB_CHECK(run_tc_fwd(Ak, mode, tc_ctas(Ak.na, Ak.ntime, Ak.nchan), stream));
+        FusedArgs<T> At = Ak;
+        if (ext_first) {
+          FusedArgs<T> Ae = Ak;
+          Ae.sbeg = Ak.npsrc;
+          Ae.partial_out = true;
+          Ae.model_vis = vis_ext;
+          Ae.chi2 = nullptr;
+          Ae.want_grad = false;
+          MB_CHECK(run_fwd(Ae, units, stream));
+          At.tc_ext = false;
+          At.accumulate_in = true;
+          At.vis_in = vis_ext;
+        }
+        MB_CHECK(run_tc_fwd(At, mode, tc_ctas(At.na, At.ntime, At.nchan), stream));
         done = true;
       }
     }
@@ -2809,7 +2844,9 @@ mb_status launch_adjoint(const FusedArgs<T>& A, mb_mode mode, double grad_scale,
 // sets' FP64 gradient accumulators (one contiguous region, cleared by one
 // memset), then per set its path-length table, sqrt(B) table (FP32), unit
 // partials, d chi^2 / dV and d chi^2 / dG.
-enum BatchKind { kBatchFwd, kBatchTcFwd, kBatchAdj, kBatchTcAdj, kBatchExtAdj };
+// kBatchExtFwd: the extended sources of split-form sets on the CUDA cores,
+// into the set's vis_ext, before their tensor-core forward.
+enum BatchKind { kBatchExtFwd, kBatchFwd, kBatchTcFwd, kBatchAdj, kBatchTcAdj, kBatchExtAdj };
 
 struct BatchGroup {
   int kind, mode, tile;
@@ -2818,7 +2855,7 @@ struct BatchGroup {
 };
 
 struct SetOffsets {
-  size_t phi, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic;
+  size_t phi, bsq0, partial, gV, dG, acc_lm, acc_stokes, acc_alpha, acc_gauss, acc_sersic, vis_ext;
 };
 
 struct BatchPlan {
@@ -2881,12 +2918,14 @@ mb_status batch_plan(mb_dtype dtype, const mb_dims* d, const mb_batch_set* sets,
     B.groups.push_back(BatchGroup{kind, mode, tile, 0, 0});
     return B.groups.back();
   };
-  for (int pass = 0; pass < 2; ++pass) {
+  for (int pass = 0; pass < 3; ++pass) {
     for (int i : B.order) {
       const mb_batch_set& s = sets[i];
       const int tile = tile_of_options(s.options);
       const bool tc = s.mode != MB_MODE_NATIVE;
       if (pass == 0) {
+        if (tc && s.ngsrc + s.nssrc > 0) group_of(kBatchExtFwd, 0, tile).count += int(units);
+      } else if (pass == 1) {
         group_of(tc ? kBatchTcFwd : kBatchFwd, tc ? int(s.mode) : 0, tile).count += int(tc ? tc_units : units);
       } else {
         if (tc && s.npsrc > 0) group_of(kBatchTcAdj, 0, 0).count += int(tc_units);
@@ -2922,6 +2961,9 @@ mb_status batch_plan(mb_dtype dtype, const mb_dims* d, const mb_batch_set* sets,
     so.partial = take(units * 8);
     so.gV = take(nt * nbl * nc * 8 * es);
     so.dG = take(nt * na * nc * 8 * es);
+    const bool ext_first = sets[i].mode != MB_MODE_NATIVE && sets[i].ngsrc + sets[i].nssrc > 0;
+    so.vis_ext = ext_first ? take(size_t(d->ntime.local_size) * d->nbl.local_size * d->nchan.local_size * 8 * es)
+                           : 0;
     B.max_phi = std::max(B.max_phi, nt * ns * na);
     B.max_bsq = std::max(B.max_bsq, ns * nt);
     B.max_grad = std::max(B.max_grad, ns * 2 + ns * nt + 3 * size_t(sets[i].ngsrc) + 3 * size_t(sets[i].nssrc) +
@@ -2966,6 +3008,8 @@ mb_status batch_prepare(const mb_dims* d, const mb_batch_set* sets, int nsets, v
     b.g_lm = static_cast<T*>(s.grads.lm); b.g_stokes = static_cast<T*>(s.grads.stokes);
     b.g_alpha = static_cast<T*>(s.grads.alpha); b.g_gauss = static_cast<T*>(s.grads.gauss_shape);
     b.g_sersic = static_cast<T*>(s.grads.sersic_shape); b.g_G = static_cast<T*>(s.grads.G_term);
+    const bool ext_first = s.mode != MB_MODE_NATIVE && s.ngsrc + s.nssrc > 0;
+    b.vis_ext = ext_first ? reinterpret_cast<T*>(w + so.vis_ext) : nullptr;
     b.npsrc = int(s.npsrc); b.ngsrc = int(s.ngsrc); b.nssrc = int(s.nssrc); b.pad = 0;
   }
   std::vector<int2> items(B.nitems);
@@ -2978,6 +3022,7 @@ mb_status batch_prepare(const mb_dims* d, const mb_batch_set* sets, int nsets, v
       const uint64_t n = uint64_t(s.npsrc) + s.ngsrc + s.nssrc;
       bool in = false;
       switch (g.kind) {
+        case kBatchExtFwd: in = tc && s.ngsrc + s.nssrc > 0 && g.tile == tile; break;
         case kBatchFwd: in = !tc && g.tile == tile; break;
         case kBatchTcFwd: in = tc && g.mode == int(s.mode) && g.tile == tile; break;
         case kBatchTcAdj: in = tc && s.npsrc > 0; break;
@@ -3033,19 +3078,31 @@ mb_status batch_run(const mb_dims* d, const mb_props* P, uint32_t options, const
       bsqrt_ref_kernel<T><<<dim3(blocks_for(B.max_bsq), nsets), 256, 0, stream>>>(A, nullptr); }
     MB_CHECK(check_launch("bsqrt_ref_kernel"));
   }
-  // forward: one launch per (form, source tile) over all its sets' units
+  // forward: one launch per (form, source tile) over all its sets' units;
+  // first the split-form sets' extended sources on the CUDA cores, which the
+  // tensor-core launch then adds its point sources to
   for (const BatchGroup& g : B.groups) {
-    if (g.kind != kBatchFwd && g.kind != kBatchTcFwd) continue;
+    if (g.kind != kBatchExtFwd && g.kind != kBatchFwd && g.kind != kBatchTcFwd) continue;
     FusedArgs<T> Ag = A;
     Ag.src_tile = g.tile;
     Ag.bitems = items + g.first;
     if constexpr (sizeof(T) == 4) {
       if (g.kind == kBatchTcFwd) {
+        Ag.tc_ext = false;
+        Ag.accumulate_in = true;  // the set's vis_ext where it has one
         MB_CHECK(run_tc_fwd(Ag, mb_mode(g.mode), g.count, stream));
         continue;
       }
     }
-    if (g.kind == kBatchFwd) MB_CHECK(run_fwd(Ag, g.count, stream));
+    if (g.kind == kBatchExtFwd) {
+      Ag.sbeg = -1;  // each set's extended sources
+      Ag.partial_out = true;  // into the set's vis_ext
+      Ag.chi2 = nullptr;
+      Ag.want_grad = false;
+      MB_CHECK(run_fwd(Ag, g.count, stream));
+    } else if (g.kind == kBatchFwd) {
+      MB_CHECK(run_fwd(Ag, g.count, stream));
+    }
   }
   if (units > 0) {
     { KernelScope ks_("sum_partials_kernel", stream);
@@ -3057,7 +3114,7 @@ mb_status batch_run(const mb_dims* d, const mb_props* P, uint32_t options, const
   // adjoint: point sources on the tensor cores, extended sources of those
   // sets, CUDA-core sets
   for (const BatchGroup& g : B.groups) {
-    if (g.kind == kBatchFwd || g.kind == kBatchTcFwd) continue;
+    if (g.kind == kBatchExtFwd || g.kind == kBatchFwd || g.kind == kBatchTcFwd) continue;
     FusedArgs<T> Ag = A;
     Ag.src_tile = g.tile;
     Ag.bitems = items + g.first;

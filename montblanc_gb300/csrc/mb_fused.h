@@ -19,6 +19,7 @@ struct BatchSet {
   T *gV, *dG;
   double *acc_lm, *acc_stokes, *acc_alpha, *acc_gauss, *acc_sersic;
   T *g_lm, *g_stokes, *g_alpha, *g_gauss, *g_sersic, *g_G;  // gradient outputs (any may be NULL)
+  T* vis_ext;  // the extended sources' visibility sums of a split-form set, or NULL
   int npsrc, ngsrc, nssrc, pad;
 };
 
@@ -48,6 +49,12 @@ struct FusedArgs {
   // outputs
   T* model_vis;
   T* chi2;
+  // Partial sums added in with accumulate_in (the caller's model_vis, or the
+  // split forms' extended-source sums in the workspace).
+  const T* vis_in;
+  // The tensor-core forward sums the extended sources itself (false: a
+  // CUDA-core launch before it has left their sums in vis_in).
+  bool tc_ext;
   // workspace
   const double* phi;  // (ntime, nsrc, na) FP64 phase path lengths
   const T* plane;     // (nchan, beam_lw, beam_mh, 12) frequency-blended beam, or NULL

@@ -171,6 +171,7 @@ def test_batch_launches_do_not_grow_with_sets():
         b.run()
         torch.cuda.synchronize()
         counts.append(_cabi.lib.mb_kernel_launches() - l0)
-    # beam plane, path lengths, sqrt(B) table, forward, chi^2 sums, point- and
-    # extended-source adjoints, gradients
-    assert counts == [8, 8], counts
+    # beam plane, path lengths, sqrt(B) table, extended sources' forward,
+    # tensor-core forward, chi^2 sums, point- and extended-source adjoints,
+    # gradients
+    assert counts == [9, 9], counts
