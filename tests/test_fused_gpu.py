@@ -36,9 +36,12 @@ def test_fused_chi2_only(dtype):
     assert abs(x2 - ref['X2']) <= TOL[dtype]['X2'] * abs(ref['X2'])
 
 
-@pytest.mark.parametrize('dtype', DTYPES)
-def test_fused_source_batches(dtype):
-    """Fused forward over two source batches accumulating in model_vis."""
+@pytest.mark.parametrize('dtype, mode', [(d, 0) for d in DTYPES] + [('float', 1)])
+def test_fused_source_batches(dtype, mode):
+    """Fused forward over two source batches accumulating in model_vis (mode
+    1, the TF32 split form: its extended sources' CUDA-core forward adds to
+    the first batch's partial sums, the tensor-core forward adds its point
+    sources to that)."""
     import montblanc_gb300 as mb
     from montblanc_gb300.rime import RimeProblem
     from montblanc_gb300 import _cabi
@@ -49,7 +52,7 @@ def test_fused_source_batches(dtype):
     vis = prob.empty_vis()
     chi2 = prob.empty_chi2()
     x2 = torch.zeros(1, dtype=torch.float64, device='cuda')
-    ws = prob.workspace('native', False)
+    ws = prob.workspace('native' if mode == 0 else 'split_tf32', False)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for lo, hi, ext in ((0, 4, {'npsrc': (0, 3), 'ngsrc': (0, 1), 'nssrc': (0, 0)}),
                         (4, 9, {'npsrc': (0, 0), 'ngsrc': (0, 2), 'nssrc': (0, 3)})):
@@ -67,7 +70,7 @@ def test_fused_source_batches(dtype):
                             extents=e, globals_={'nsrc': 9})
         d.nsrc.local_size = 9
         inp = prob.inputs(**ov)
-        _cabi.call('mb_rime_forward', prob.mb_dtype, 0, ctypes.byref(d), ctypes.byref(prob.mb_props()),
+        _cabi.call('mb_rime_forward', prob.mb_dtype, mode, ctypes.byref(d), ctypes.byref(prob.mb_props()),
                    prob.options(), ctypes.byref(inp), vis.data_ptr(), chi2.data_ptr(), x2.data_ptr(), 0,
                    ws.data_ptr(), ws.numel(), stream)
     assert golden_io.rel_err(vis.cpu().numpy(), ref['vis_out']) < TOL[dtype]['vis']
