@@ -2731,6 +2731,10 @@ mb_status run_adj(const FusedArgs<T>& A, bool ext_only, int grid, cudaStream_t s
   if (S.total > kMaxDynamicSmem)
     return fail(MB_ERR_UNSUPPORTED, "fused adjoint needs %zu bytes of shared memory for na=%d", S.total, A.na);
   if (grid == 0) return MB_OK;
+  // Where the shared memory of two CTAs fits an SM, CTAs of half the threads
+  // (the registers of one 512-thread CTA): two per SM, so that one computes
+  // while the other waits at its tile barriers.
+  if (sizeof(T) == 4 && 2 * S.total <= kMaxDynamicSmem) S.nthreads = AdjTile<T>::THREADS / 2;
   auto kern = A.bitems ? coh_adj_kernel<T, RA, RS, true> : coh_adj_kernel<T, RA, RS, false>;
   MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S.total)));
   { KernelScope ks_("coh_adj_kernel", stream); kern<<<grid, S.nthreads, S.total, stream>>>(A, S); }
