@@ -270,6 +270,38 @@ template <> __device__ __forceinline__ Cx<float> phase_from_cycles<float>(double
   return {c, s};
 }
 
+// An FP64 value as the FP32 pair (hi, lo) = (float(x), float(x - hi)):
+// 48 significant bits in the 8 bytes of the double.
+__device__ __forceinline__ float2 split_f64(double x) {
+  const float h = float(x);
+  return make_float2(h, float(x - double(h)));
+}
+
+// cycles = phi nu / c reduced to about [-1/2, 1/2], from the FP32 pairs
+// (ph, pl) of phi and (nh, nl) of nu / c, on the FP32 pipe only.  With p the
+// rounded product ph nh, e0 = ph nh - p is exact (one FMA), p - rint(p) is
+// exact (Sterbenz), and the small terms e0 + ph nl + pl nh are added to it;
+// the dropped pl nl and the pairs' own truncation leave an absolute error
+// of about |cycles| 2^-47 before the final FP32 rounding (2^-25): 4e-10
+// cycles at |cycles| = 5e4.  (The FP64 product and its exact reduction
+// leave |cycles| 2^-53.)  p is formed by __fmul_rn so that it is not fused
+// into the subtraction, which would count e0 twice.
+__device__ __forceinline__ float frac_cycles_df(float ph, float pl, float nh, float nl) {
+  const float p = __fmul_rn(ph, nh);
+  float e = fmaf(ph, nh, -p);
+  e = fmaf(ph, nl, e);
+  e = fmaf(pl, nh, e);
+  return __fadd_rn(__fsub_rn(p, rintf(p)), e);
+}
+
+// K from the pair of the path length (as split_f64 stores it) and nu / c.
+__device__ __forceinline__ Cx<float> phase_from_pair(float2 phi, double nu_over_c) {
+  const float2 n = split_f64(nu_over_c);
+  float s, c;
+  sincospif(-2.0f * frac_cycles_df(phi.x, phi.y, n.x, n.y), &s, &c);
+  return {c, s};
+}
+
 // ---- beam cube (a3) ------------------------------------------------------
 // Beam grid position along one axis: scale * (x - lower), clamped to
 // [0, n-1], split into the lower grid index, the upper grid index and the

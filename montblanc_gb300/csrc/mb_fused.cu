@@ -287,11 +287,19 @@ __device__ void load_sources(const FusedArgs<T>& A, int t, int ch, int s0, int n
   for (int i = threadIdx.x; i < ns; i += blockDim.x) ss[i] = load_source_one(A, t, ch, s0 + i);
 }
 
+// K(s, a) at time t.  The path-length table (phi_kernel) holds FP64 values
+// for the FP64 forms and, in the same 8 bytes per entry, the FP32 pair of
+// the same FP64 value (split_f64) for the FP32 forms, whose phase is then
+// formed on the FP32 pipe (frac_cycles_df).
 template <typename T>
 __device__ __forceinline__ Cx<T> phase_term(const FusedArgs<T>& A, int t, int s, int a, T f, double nu_over_c) {
   double phi;
+  const size_t e = (size_t(t) * A.nsrc + s) * A.na_glob + gant(A, a);
+  if constexpr (sizeof(T) == 4) {
+    if (A.phi != nullptr) return phase_from_pair(__ldg(reinterpret_cast<const float2*>(A.phi) + e), nu_over_c);
+  }
   if (A.phi != nullptr) {
-    phi = A.phi[(size_t(t) * A.nsrc + s) * A.na_glob + gant(A, a)];
+    phi = A.phi[e];
   } else {  // no table: the same FP64 path length, formed in place
     double l = A.lm[2 * s], m = A.lm[2 * s + 1];
     double n = sqrt(1.0 - l * l - m * m) - 1.0;
@@ -2349,7 +2357,9 @@ __global__ void phi_kernel(FusedArgs<T> A_in, double* __restrict__ phi) {
     double l = A.lm[2 * s], m = A.lm[2 * s + 1];
     double n = sqrt(1.0 - l * l - m * m) - 1.0;
     const T* p = A.uvw + 3 * (size_t(t) * A.lna + a);
-    phi[i] = l * double(p[0]) + m * double(p[1]) + n * double(p[2]);
+    const double v = l * double(p[0]) + m * double(p[1]) + n * double(p[2]);
+    if constexpr (sizeof(T) == 4) reinterpret_cast<float2*>(phi)[i] = split_f64(v);  // see phase_term
+    else phi[i] = v;
   }
 }
 
