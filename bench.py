@@ -696,7 +696,7 @@ def run_config(args, ws):
     nvis = w['ntime'] * synth.nr_of_baselines(w['na']) * w['nchan']
     return {'workload': workload_desc(args.workload), 'mode': args.mode, 'terms_per_step': terms_of(args.workload),
             'l2': 'inputs larger than L2 (observed_vis alone %.1f GB)' % (nvis * 4 * 8 / 1e9),
-            'phase': 'FP64 argument and range reduction', 'replicas': ws}
+            'phase': 'FP64 path length; FP32 forms reduce phi nu / c as a double-float product', 'replicas': ws}
 
 
 def main():

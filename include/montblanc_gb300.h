@@ -47,7 +47,11 @@ typedef enum mb_dtype { MB_FLOAT32 = 0, MB_FLOAT64 = 1 } mb_dtype;
  * MB_MODE_SPLIT_TF32 / MB_MODE_SPLIT_BF16: point sources as a per-(time,
  * channel) complex GEMM on the tensor cores, operands split into hi + lo
  * parts (3 products, FP32 accumulation); FLOAT32 data only.
- * In every mode the phase argument and its range reduction run in FP64. */
+ * In every mode the path length u l + v m + w (n - 1) is formed in FP64.
+ * The FP64 mode forms the phase argument in FP64; the FP32 modes form it
+ * and its reduction to [-1/2, 1/2] cycles from FP32 pairs (hi, lo) of the
+ * path length and of nu / c (about 47 significant bits; an absolute error
+ * near |cycles| 2^-47), then take an FP32 sincospi of the reduced value. */
 typedef enum mb_mode {
   MB_MODE_NATIVE = 0,
   MB_MODE_SPLIT_TF32 = 1,

@@ -285,7 +285,10 @@ __device__ __forceinline__ float2 split_f64(double x) {
 // of about |cycles| 2^-47 before the final FP32 rounding (2^-25): 4e-10
 // cycles at |cycles| = 5e4.  (The FP64 product and its exact reduction
 // leave |cycles| 2^-53.)  p is formed by __fmul_rn so that it is not fused
-// into the subtraction, which would count e0 twice.
+// into the subtraction, which would count e0 twice.  The result lies within
+// 3 |p| 2^-24 of [-1/2, 1/2] (the three small terms are each at most about
+// |p| 2^-24; above 2^23 cycles p is an integer and they are all that is
+// left); the sincospi that takes it reduces the rest exactly.
 __device__ __forceinline__ float frac_cycles_df(float ph, float pl, float nh, float nl) {
   const float p = __fmul_rn(ph, nh);
   float e = fmaf(ph, nh, -p);
