@@ -421,19 +421,29 @@ template <typename T, bool DERIV>
 __device__ __forceinline__ void plane_cell(const T* __restrict__ p, T x, T y, T (&v)[kPlaneComp],
                                            T (&dx)[kPlaneComp], T (&dy)[kPlaneComp]) {
   if constexpr (sizeof(T) == 4) {
+    // two values per packed FP32x2 FMA (each lane rounded as fmaf)
     const float4* q = reinterpret_cast<const float4*>(p);
+    const float2 xx = make_float2(x, x), yy = make_float2(y, y);
 #pragma unroll
     for (int r = 0; r < 3; ++r) {  // float4 runs: E.a E.b | E.c E.d | |E|
       const float4 f4 = __ldg(q + r), a4 = __ldg(q + 3 + r), b4 = __ldg(q + 6 + r), c4 = __ldg(q + 9 + r);
-      const float f[4] = {f4.x, f4.y, f4.z, f4.w}, a[4] = {a4.x, a4.y, a4.z, a4.w};
-      const float b[4] = {b4.x, b4.y, b4.z, b4.w}, c[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float fy = fmaf(x, c[k], b[k]);
-        v[4 * r + k] = fmaf(y, fy, fmaf(x, a[k], f[k]));
+      for (int h = 0; h < 2; ++h) {
+        const float2 f = h ? make_float2(f4.z, f4.w) : make_float2(f4.x, f4.y);
+        const float2 a = h ? make_float2(a4.z, a4.w) : make_float2(a4.x, a4.y);
+        const float2 b = h ? make_float2(b4.z, b4.w) : make_float2(b4.x, b4.y);
+        const float2 c = h ? make_float2(c4.z, c4.w) : make_float2(c4.x, c4.y);
+        const float2 fy = __ffma2_rn(xx, c, b);
+        const float2 vv = __ffma2_rn(yy, fy, __ffma2_rn(xx, a, f));
+        const int k = 4 * r + 2 * h;
+        v[k] = vv.x;
+        v[k + 1] = vv.y;
         if (DERIV) {
-          dx[4 * r + k] = fmaf(y, c[k], a[k]);
-          dy[4 * r + k] = fy;
+          const float2 d = __ffma2_rn(yy, c, a);
+          dx[k] = d.x;
+          dx[k + 1] = d.y;
+          dy[k] = fy.x;
+          dy[k + 1] = fy.y;
         }
       }
     }

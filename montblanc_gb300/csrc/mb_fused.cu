@@ -1460,11 +1460,21 @@ __device__ void beam_interp_plane_d(const T* __restrict__ plane, int mh, const G
     T inv = mb_rsqrt(s4.r * s4.r + s4.i * s4.i);
     inv = isfinite(inv) ? inv : T(1);
     const T g = amp * inv, gi = g * inv;
-    E4[k] = s4 * g;
     const T hl = inv * (dal - gi * cdot_re(s4, l4));
     const T hm = inv * (dam - gi * cdot_re(s4, m4));
-    dl4[k] = {l4.r * g + s4.r * hl, l4.i * g + s4.i * hl};
-    dm4[k] = {m4.r * g + s4.r * hm, m4.i * g + s4.i * hm};
+    if constexpr (sizeof(T) == 4) {  // (Re, Im) pairs by packed FP32x2 arithmetic
+      const float2 s2 = make_float2(s4.r, s4.i), gg = make_float2(g, g);
+      const float2 e = __fmul2_rn(s2, gg);
+      const float2 dl = __ffma2_rn(s2, make_float2(hl, hl), __fmul2_rn(make_float2(l4.r, l4.i), gg));
+      const float2 dm = __ffma2_rn(s2, make_float2(hm, hm), __fmul2_rn(make_float2(m4.r, m4.i), gg));
+      E4[k] = {e.x, e.y};
+      dl4[k] = {dl.x, dl.y};
+      dm4[k] = {dm.x, dm.y};
+    } else {
+      E4[k] = s4 * g;
+      dl4[k] = {l4.r * g + s4.r * hl, l4.i * g + s4.i * hl};
+      dm4[k] = {m4.r * g + s4.r * hm, m4.i * g + s4.i * hm};
+    }
   }
 }
 
