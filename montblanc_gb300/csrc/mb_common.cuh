@@ -53,6 +53,32 @@ template <typename T> __device__ __forceinline__ void cmacc(Cx<T>& acc, Cx<T> a,
 // Re(conj(a) * b)
 template <typename T> __device__ __forceinline__ T cdot_re(Cx<T> a, Cx<T> b) { return a.r * b.r + a.i * b.i; }
 
+// FP32: a complex value is an FP32x2 pair (re, im) for the packed FMAs of
+// sm_100 and later (each lane rounded as fmaf).  An operand may be a
+// broadcast scalar, the swapped pair or have one lane negated at no extra
+// instruction, so a complex product or multiply-add is 2 instructions
+// instead of 4.
+__device__ __forceinline__ float2 as_f2(Cx<float> z) { return make_float2(z.r, z.i); }
+__device__ __forceinline__ Cx<float> as_cx(float2 v) { return {v.x, v.y}; }
+// (a.r b.r - a.i b.i, a.i b.r + a.r b.i)
+template <> __device__ __forceinline__ Cx<float> cmul<float>(Cx<float> a, Cx<float> b) {
+  const float2 p = __fmul2_rn(as_f2(a), make_float2(b.r, b.r));
+  return as_cx(__ffma2_rn(make_float2(a.i, a.r), make_float2(-b.i, b.i), p));
+}
+// (a.r b.r + a.i b.i, a.i b.r - a.r b.i)
+template <> __device__ __forceinline__ Cx<float> cmulc<float>(Cx<float> a, Cx<float> b) {
+  const float2 p = __fmul2_rn(as_f2(a), make_float2(b.r, b.r));
+  return as_cx(__ffma2_rn(make_float2(a.i, a.r), make_float2(b.i, -b.i), p));
+}
+template <> __device__ __forceinline__ void cmac<float>(Cx<float>& acc, Cx<float> a, Cx<float> b) {
+  float2 p = __ffma2_rn(make_float2(a.i, a.r), make_float2(-b.i, b.i), as_f2(acc));
+  acc = as_cx(__ffma2_rn(as_f2(a), make_float2(b.r, b.r), p));
+}
+template <> __device__ __forceinline__ void cmacc<float>(Cx<float>& acc, Cx<float> a, Cx<float> b) {
+  float2 p = __ffma2_rn(make_float2(a.i, a.r), make_float2(b.i, -b.i), as_f2(acc));
+  acc = as_cx(__ffma2_rn(as_f2(a), make_float2(b.r, b.r), p));
+}
+
 // 2x2 complex Jones matrix, row-major [00, 01, 10, 11].
 template <typename T>
 struct Jones {
@@ -120,6 +146,13 @@ template <typename T> __device__ __forceinline__ Jones<T> jherm(const Jones<T>& 
 template <typename T> __device__ __forceinline__ T jdot_re(const Jones<T>& X, const Jones<T>& Y) {
   return cdot_re(X.a, Y.a) + cdot_re(X.b, Y.b) + cdot_re(X.c, Y.c) + cdot_re(X.d, Y.d);
 }
+template <> __device__ __forceinline__ float jdot_re<float>(const Jones<float>& X, const Jones<float>& Y) {
+  float2 p = __fmul2_rn(as_f2(X.a), as_f2(Y.a));
+  p = __ffma2_rn(as_f2(X.b), as_f2(Y.b), p);
+  p = __ffma2_rn(as_f2(X.c), as_f2(Y.c), p);
+  p = __ffma2_rn(as_f2(X.d), as_f2(Y.d), p);
+  return p.x + p.y;
+}
 
 // ---- loads / stores of interleaved complex Jones -------------------------
 template <typename T> __device__ __forceinline__ Jones<T> jload(const T* p);
@@ -184,6 +217,25 @@ template <typename T>
 __device__ __forceinline__ Jones<T> jmul_herm_real_diag(const Jones<T>& X, T a, T d, Cx<T> b) {
   const Cx<T> bc = conj(b);
   return {X.a * a + cmul(X.b, bc), cmul(X.a, b) + X.b * d, X.c * a + cmul(X.d, bc), cmul(X.c, b) + X.d * d};
+}
+// Row (x0, x1) of X times [[a, b], [conj b, d]] is (x0 a + x1 conj b, x0 b + x1 d).
+template <>
+__device__ __forceinline__ Jones<float> jmul_herm_real_diag<float>(const Jones<float>& X, float a, float d,
+                                                                   Cx<float> b) {
+  Jones<float> R;
+  const Cx<float>* x = &X.a;
+  Cx<float>* y = &R.a;
+#pragma unroll
+  for (int row = 0; row < 2; ++row) {
+    const Cx<float> x0 = x[2 * row], x1 = x[2 * row + 1];
+    float2 p = __fmul2_rn(as_f2(x0), make_float2(a, a));
+    p = __ffma2_rn(as_f2(x1), make_float2(b.r, b.r), p);
+    y[2 * row] = as_cx(__ffma2_rn(make_float2(x1.i, x1.r), make_float2(b.i, -b.i), p));
+    float2 q = __fmul2_rn(as_f2(x1), make_float2(d, d));
+    q = __ffma2_rn(as_f2(x0), make_float2(b.r, b.r), q);
+    y[2 * row + 1] = as_cx(__ffma2_rn(make_float2(x0.i, x0.r), make_float2(-b.i, b.i), q));
+  }
+  return R;
 }
 
 // ---- brightness square root (a1) -----------------------------------------
