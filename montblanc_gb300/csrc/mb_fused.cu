@@ -891,16 +891,19 @@ struct TcPlan {
   int group;
 };
 
-// Adds a drained group sum x to the pair accumulator *hi and returns the
-// rounding error of the addition.  Fast2Sum: x - ((hi + x) - hi) is exact
-// when |hi| >= |x|, the usual case (hi is the sum over all earlier groups;
-// also exact while hi is 0); otherwise it is off by at most an ulp of the
-// sum, the error of one plain FP32 addition.
-__device__ __forceinline__ float fold_carry(float* hi, float x) {
-  const float a = *hi;
-  const float sum = a + x;
-  *hi = sum;
-  return x - (sum - a);
+// Adds drained group sums x.x, x.y to the pair accumulators *h0, *h1 and
+// returns the rounding errors of the additions (packed FP32x2 adds).
+// Fast2Sum: x - ((h + x) - h) is exact when |h| >= |x|, the usual case (h
+// is the sum over all earlier groups; also exact while h is 0); otherwise
+// it is off by at most an ulp of the sum, the error of one plain FP32
+// addition.
+__device__ __forceinline__ float2 fold_carry2(float* h0, float* h1, float2 x) {
+  const float2 a = make_float2(*h0, *h1);
+  const float2 sum = __fadd2_rn(a, x);
+  *h0 = sum.x;
+  *h1 = sum.y;
+  const float2 d = __fadd2_rn(sum, make_float2(-a.x, -a.y));
+  return __fadd2_rn(x, make_float2(-d.x, -d.y));
 }
 
 // Drain TMEM into the FP32 pair accumulators (all 12 warps): a warp reads
@@ -955,23 +958,28 @@ __device__ void tc_drain(const FusedArgs<float>& A, uint32_t tmem, float* sVf, b
     float v[32], w[32];
     tc::tmem_ld32x2(lane_addr + 32 * blk, lane_addr + 256 + 32 * blk, v, w);
 #pragma unroll
-    for (int k = 0; k < 32; ++k) {
-      v[k] += w[k];  // main + correction accumulators
-      w[k] = 0.f;    // carries
+    for (int k = 0; k < 32; k += 2) {
+      const float2 m = __fadd2_rn(make_float2(v[k], v[k + 1]), make_float2(w[k], w[k + 1]));  // main + correction
+      v[k] = m.x;
+      v[k + 1] = m.y;
+      w[k] = w[k + 1] = 0.f;  // carries
     }
     if (need) {
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
         const int b = b_lo + c;
+        const float2 x = make_float2(v[2 * c], v[2 * c + 1]);
+        float2 r = make_float2(0.f, 0.f);
         if (b >= a && b <= up_hi) {
           const int e = ku + 8 * b;
-          w[2 * c] = fold_carry(sVf + e, v[2 * c]);
-          w[2 * c + 1] = fold_carry(sVf + e + 2, v[2 * c + 1]);
+          r = fold_carry2(sVf + e, sVf + e + 2, x);
         } else if (b <= wrap_end) {
           const int e = 8 * (b * na - (b * (b - 1)) / 2 - b) + kl;
-          w[2 * c] = sgn * fold_carry(sVf + e, sgn * v[2 * c]);
-          w[2 * c + 1] = sgn * fold_carry(sVf + e + 4, sgn * v[2 * c + 1]);
+          r = fold_carry2(sVf + e, sVf + e + 4, make_float2(sgn * x.x, sgn * x.y));
+          r = make_float2(sgn * r.x, sgn * r.y);
         }
+        w[2 * c] = r.x;
+        w[2 * c + 1] = r.y;
       }
     }
     if (carry) {

@@ -54,12 +54,11 @@ struct StageLayout<MB_MODE_SPLIT_TF32, ROWB, LBO, SBO> : StageGeometry<ROWB, LBO
   // Two consecutive values (k even).
   __device__ __forceinline__ static void put2(unsigned char* hi, unsigned char* lo, int row, int k, float x0,
                                               float x1) {
-    float h0, l0, h1, l1;
-    tc::split_tf32(x0, h0, l0);
-    tc::split_tf32(x1, h1, l1);
+    float2 h, l;
+    tc::split_tf32x2(x0, x1, h, l);
     const uint32_t o = G::offset(row, k * kElem);
-    *reinterpret_cast<float2*>(hi + o) = make_float2(h0, h1);
-    *reinterpret_cast<float2*>(lo + o) = make_float2(l0, l1);
+    *reinterpret_cast<float2*>(hi + o) = h;
+    *reinterpret_cast<float2*>(lo + o) = l;
   }
 };
 
@@ -81,12 +80,9 @@ struct StageLayout<MB_MODE_SPLIT_BF16, ROWB, LBO, SBO> : StageGeometry<ROWB, LBO
   }
   __device__ __forceinline__ static void put2(unsigned char* hi, unsigned char* lo, int row, int k, float x0,
                                               float x1) {
-    __nv_bfloat16 h0, l0, h1, l1;
-    tc::split_bf16(x0, h0, l0);
-    tc::split_bf16(x1, h1, l1);
-    const uint32_t o = G::offset(row, k * kElem);
     __nv_bfloat162 hh, ll;
-    hh.x = h0; hh.y = h1; ll.x = l0; ll.y = l1;
+    tc::split_bf16x2(x0, x1, hh, ll);
+    const uint32_t o = G::offset(row, k * kElem);
     *reinterpret_cast<__nv_bfloat162*>(hi + o) = hh;
     *reinterpret_cast<__nv_bfloat162*>(lo + o) = ll;
   }

@@ -202,5 +202,26 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
   lo = __float2bfloat16_rn(x - __bfloat162float(hi));
 }
 
+// Both splits for two values at once: the residuals x - hi (exact) by one
+// packed FP32x2 add; for BF16 also the two conversions of each part by one
+// bf16x2 conversion.  Same results as two scalar splits.
+__device__ __forceinline__ void split_tf32x2(float x0, float x1, float2& hi, float2& lo) {
+  uint32_t h0, h1, l0, l1;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h0) : "f"(x0));
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h1) : "f"(x1));
+  hi = make_float2(__uint_as_float(h0), __uint_as_float(h1));
+  const float2 r = __fadd2_rn(make_float2(x0, x1), make_float2(-hi.x, -hi.y));
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l0) : "f"(r.x));
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l1) : "f"(r.y));
+  lo = make_float2(__uint_as_float(l0), __uint_as_float(l1));
+}
+
+__device__ __forceinline__ void split_bf16x2(float x0, float x1, __nv_bfloat162& hi, __nv_bfloat162& lo) {
+  hi = __floats2bfloat162_rn(x0, x1);
+  const float2 h = __bfloat1622float2(hi);
+  const float2 r = __fadd2_rn(make_float2(x0, x1), make_float2(-h.x, -h.y));
+  lo = __floats2bfloat162_rn(r.x, r.y);
+}
+
 }  // namespace tc
 }  // namespace mb
