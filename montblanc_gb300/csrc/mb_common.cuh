@@ -96,6 +96,22 @@ template <typename T> __device__ __forceinline__ Jones<T> jadd(const Jones<T>& x
 template <typename T> __device__ __forceinline__ Jones<T> jscale(const Jones<T>& x, T s) {
   return {x.a * s, x.b * s, x.c * s, x.d * s};
 }
+template <> __device__ __forceinline__ Jones<float> jscale<float>(const Jones<float>& x, float s) {
+  const float2 ss = make_float2(s, s);
+  return {as_cx(__fmul2_rn(as_f2(x.a), ss)), as_cx(__fmul2_rn(as_f2(x.b), ss)), as_cx(__fmul2_rn(as_f2(x.c), ss)),
+          as_cx(__fmul2_rn(as_f2(x.d), ss))};
+}
+// acc += x s
+template <typename T> __device__ __forceinline__ void jaxpy(Jones<T>& acc, const Jones<T>& x, T s) {
+  acc = jadd(acc, jscale(x, s));
+}
+template <> __device__ __forceinline__ void jaxpy<float>(Jones<float>& acc, const Jones<float>& x, float s) {
+  const float2 ss = make_float2(s, s);
+  acc.a = as_cx(__ffma2_rn(as_f2(x.a), ss, as_f2(acc.a)));
+  acc.b = as_cx(__ffma2_rn(as_f2(x.b), ss, as_f2(acc.b)));
+  acc.c = as_cx(__ffma2_rn(as_f2(x.c), ss, as_f2(acc.c)));
+  acc.d = as_cx(__ffma2_rn(as_f2(x.d), ss, as_f2(acc.d)));
+}
 // X * Y
 template <typename T> __device__ __forceinline__ Jones<T> jmul(const Jones<T>& X, const Jones<T>& Y) {
   Jones<T> R;

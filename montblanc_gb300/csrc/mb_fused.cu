@@ -1692,7 +1692,7 @@ __device__ void adj_ext_tile(const FusedArgs<T>& A, const SmemPlan& S, int t, in
         const Jones<T> P = jmul(y_at(sX, a, b, A.na), *jtile(sJ, S, si, b));
         T d[3];
         const T c = shape_and_grad<T>(src.type, sa[b].u - ua, sa[b].v - va, src.s0, src.s1, src.s2, kg, ks, d);
-        acc = jadd(acc, jscale(P, c));
+        jaxpy(acc, P, c);
         if (a < b) {
           const T gc = jdot_re(Ja, P);
           g[7] += gc * d[0]; g[8] += gc * d[1]; g[9] += gc * d[2];
