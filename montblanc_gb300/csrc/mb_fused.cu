@@ -340,13 +340,13 @@ __device__ void produce_jones(const FusedArgs<T>& A, const SmemPlan& S, int t, i
     int si = i / S.nap, a = i - si * S.nap;
     const Jones<T> J = a < A.na ? compute_jones(A, t, s0 + si, a, ss[si], sa[a], f, nu_over_c, cp, ch)
                                 : jzero<T>();
-    if constexpr (DF && sizeof(T) == 8) {
+    if constexpr (DF && sizeof(T) == 8) {  // per entry (re hi, im hi, re lo, im lo)
       const double* v = reinterpret_cast<const double*>(&J);
-      float2* o = reinterpret_cast<float2*>(jtile(sJ, S, si, a));
+      float4* o = reinterpret_cast<float4*>(jtile(sJ, S, si, a));
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const float h = float(v[k]);
-        o[k] = make_float2(h, float(v[k] - double(h)));
+      for (int k = 0; k < 4; ++k) {
+        const float hr = float(v[2 * k]), hi = float(v[2 * k + 1]);
+        o[k] = make_float4(hr, hi, float(v[2 * k] - double(hr)), float(v[2 * k + 1] - double(hi)));
       }
     } else {
       *jtile(sJ, S, si, a) = J;
@@ -559,53 +559,40 @@ __device__ __forceinline__ void fold_pair(Jones<T>* sV, Jones<T>* sVlo, const Jo
 // use values held as hi + lo FP32 pairs (about 48 significant bits): an
 // exact product by FMA (Dekker's product, with the cross terms of the low
 // parts) added to the accumulator by TwoSum (Knuth), 11 FP32 operations per
-// multiply-add against one FP64 FMA; per tile the sums are converted to
-// FP64 and folded into the FP64 pair accumulators.  The per-antenna terms
-// J and the shape factors are formed in FP64.
-struct Df {
-  float h, l;
-};
+// multiply-add against one FP64 FMA, and the real and imaginary parts of a
+// complex value share packed FP32x2 instructions, so a complex multiply-add
+// takes 24 of them; per tile the sums are converted to FP64 and folded into
+// the FP64 pair accumulators.  The per-antenna terms J and the shape factors
+// are formed in FP64.
+//
+// A complex double-float value: h = (re hi, im hi), l = (re lo, im lo).
 struct CDf {
-  Df r, i;
+  float2 h, l;
 };
 struct JDf {
   CDf a, b, c, d;
 };
 
-__device__ __forceinline__ Df df_of(double x) {
-  const float h = float(x);
-  return {h, float(x - double(h))};
-}
-__device__ __forceinline__ double df_value(Df x) { return double(x.h) + double(x.l); }
-
-// acc += a * b
-__device__ __forceinline__ void df_mac(Df& acc, Df a, Df b) {
-  const float p = a.h * b.h;
-  float e = fmaf(a.h, b.h, -p);
-  e = fmaf(a.h, b.l, e);
-  e = fmaf(a.l, b.h, e);
-  const float s = acc.h + p;
-  const float v = s - acc.h;
-  const float t = (acc.h - (s - v)) + (p - v);
+// acc += x * (bh + bl): per lane, Dekker's product of x and the scalar
+// double-float b (exact by FMA, with the cross terms of the low parts), added
+// to acc by TwoSum.  12 packed instructions for the two lanes.
+__device__ __forceinline__ void cdf_mac(CDf& acc, float2 xh, float2 xl, float bh, float bl) {
+  const float2 bh2 = make_float2(bh, bh), bl2 = make_float2(bl, bl);
+  const float2 p = __fmul2_rn(xh, bh2);
+  float2 e = __ffma2_rn(xh, bh2, make_float2(-p.x, -p.y));
+  e = __ffma2_rn(xh, bl2, e);
+  e = __ffma2_rn(xl, bh2, e);
+  const float2 s = __fadd2_rn(acc.h, p);
+  const float2 v = __fadd2_rn(s, make_float2(-acc.h.x, -acc.h.y));
+  const float2 sv = __fadd2_rn(s, make_float2(-v.x, -v.y));
+  const float2 t = __fadd2_rn(__fadd2_rn(acc.h, make_float2(-sv.x, -sv.y)), __fadd2_rn(p, make_float2(-v.x, -v.y)));
   acc.h = s;
-  acc.l += t + e;
+  acc.l = __fadd2_rn(acc.l, __fadd2_rn(t, e));
 }
-__device__ __forceinline__ Df df_neg(Df a) { return {-a.h, -a.l}; }
-// a * b rounded back to a double-float (the product's low part kept)
-__device__ __forceinline__ Df df_mul(Df a, Df b) {
-  const float p = a.h * b.h;
-  float e = fmaf(a.h, b.h, -p);
-  e = fmaf(a.h, b.l, e);
-  e = fmaf(a.l, b.h, e);
-  const float s = p + e;
-  return {s, e - (s - p)};
-}
-// acc += a * conj(b)
+// acc += a * conj(b) = (a.r, a.i) b.r + (a.i, -a.r) b.i
 __device__ __forceinline__ void cmacc_df(CDf& acc, const CDf& a, const CDf& b) {
-  df_mac(acc.r, a.r, b.r);
-  df_mac(acc.r, a.i, b.i);
-  df_mac(acc.i, a.i, b.r);
-  df_mac(acc.i, df_neg(a.r), b.i);
+  cdf_mac(acc, a.h, a.l, b.h.x, b.l.x);
+  cdf_mac(acc, make_float2(a.h.y, -a.h.x), make_float2(a.l.y, -a.l.x), b.h.y, b.l.y);
 }
 // acc += X * Y^H
 __device__ __forceinline__ void jmac_h_df(JDf& acc, const JDf& X, const JDf& Y) {
@@ -617,30 +604,41 @@ __device__ __forceinline__ void jmac_h_df(JDf& acc, const JDf& X, const JDf& Y) 
 // A Jones tile entry written by produce_jones<double, true>.
 __device__ __forceinline__ JDf jdf_load(const Jones<double>* p) {
   const float4* q = reinterpret_cast<const float4*>(p);
-  const float4 x0 = q[0], x1 = q[1], x2 = q[2], x3 = q[3];
   JDf J;
-  J.a.r = {x0.x, x0.y}; J.a.i = {x0.z, x0.w};
-  J.b.r = {x1.x, x1.y}; J.b.i = {x1.z, x1.w};
-  J.c.r = {x2.x, x2.y}; J.c.i = {x2.z, x2.w};
-  J.d.r = {x3.x, x3.y}; J.d.i = {x3.z, x3.w};
+  CDf* e = &J.a;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float4 x = q[k];
+    e[k] = {make_float2(x.x, x.y), make_float2(x.z, x.w)};
+  }
   return J;
 }
 __device__ __forceinline__ JDf jdf_zero() {
   JDf J;
-  J.a.r = J.a.i = J.b.r = J.b.i = J.c.r = J.c.i = J.d.r = J.d.i = Df{0.f, 0.f};
+  J.a = J.b = J.c = J.d = CDf{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
   return J;
 }
-__device__ __forceinline__ JDf jdf_scale(const JDf& X, Df s) {
-  JDf R;
-  R.a.r = df_mul(X.a.r, s); R.a.i = df_mul(X.a.i, s);
-  R.b.r = df_mul(X.b.r, s); R.b.i = df_mul(X.b.i, s);
-  R.c.r = df_mul(X.c.r, s); R.c.i = df_mul(X.c.i, s);
-  R.d.r = df_mul(X.d.r, s); R.d.i = df_mul(X.d.i, s);
-  return R;
+// x * s, s an FP64 scalar, rounded back to double-float per lane (the
+// product's low part kept)
+__device__ __forceinline__ CDf cdf_scale(const CDf& x, float sh, float sl) {
+  const float2 sh2 = make_float2(sh, sh), sl2 = make_float2(sl, sl);
+  const float2 p = __fmul2_rn(x.h, sh2);
+  float2 e = __ffma2_rn(x.h, sh2, make_float2(-p.x, -p.y));
+  e = __ffma2_rn(x.h, sl2, e);
+  e = __ffma2_rn(x.l, sh2, e);
+  const float2 s = __fadd2_rn(p, e);
+  const float2 d = __fadd2_rn(s, make_float2(-p.x, -p.y));
+  return {s, __fadd2_rn(e, make_float2(-d.x, -d.y))};
+}
+__device__ __forceinline__ JDf jdf_scale(const JDf& X, double s) {
+  const float sh = float(s), sl = float(s - double(sh));
+  return {cdf_scale(X.a, sh, sl), cdf_scale(X.b, sh, sl), cdf_scale(X.c, sh, sl), cdf_scale(X.d, sh, sl)};
+}
+__device__ __forceinline__ Cx<double> cdf_value(const CDf& x) {
+  return {double(x.h.x) + double(x.l.x), double(x.h.y) + double(x.l.y)};
 }
 __device__ __forceinline__ Jones<double> jdf_value(const JDf& X) {
-  return {{df_value(X.a.r), df_value(X.a.i)}, {df_value(X.b.r), df_value(X.b.i)},
-          {df_value(X.c.r), df_value(X.c.i)}, {df_value(X.d.r), df_value(X.d.i)}};
+  return {cdf_value(X.a), cdf_value(X.b), cdf_value(X.c), cdf_value(X.d)};
 }
 
 // consume_pairs for the FP64 forward on double-float Jones tiles (same work
@@ -689,7 +687,7 @@ __device__ void consume_pairs_df(const FusedArgs<double>& A, const SmemPlan& S, 
 #pragma unroll
             for (int c = 0; c < RQ; ++c) {
               const double sh = shape_factor<double>(src.type, u[r][c], v[r][c], src.s0, src.s1, src.s2, kg, ks);
-              jmac_h_df(acc[r][c], jdf_scale(Ja[r], df_of(sh)), Jb[c]);
+              jmac_h_df(acc[r][c], jdf_scale(Ja[r], sh), Jb[c]);
             }
         }
       }
