@@ -365,12 +365,23 @@ __device__ __forceinline__ float frac_cycles_df(float ph, float pl, float nh, fl
   return __fadd_rn(__fsub_rn(p, rintf(p)), e);
 }
 
-// K from the pair of the path length (as split_f64 stores it) and nu / c.
-__device__ __forceinline__ Cx<float> phase_from_pair(float2 phi, double nu_over_c) {
-  const float2 n = split_f64(nu_over_c);
+// K from the pairs of the path length (as split_f64 stores it) and of nu / c.
+__device__ __forceinline__ Cx<float> phase_from_pair(float2 phi, float2 n) {
   float s, c;
   sincospif(-2.0f * frac_cycles_df(phi.x, phi.y, n.x, n.y), &s, &c);
   return {c, s};
+}
+
+// nu / c of one channel with what the per-item terms take from it formed
+// once per channel (FP64 arithmetic costs 64 FP32 operations on GB300):
+// its FP32 pair for phase_from_pair and 2 pi nu / c = |dK/dphi|.
+struct NuC {
+  double d;
+  float2 p;
+  double dphase;
+};
+__device__ __forceinline__ NuC make_nuc(double nu_over_c) {
+  return {nu_over_c, split_f64(nu_over_c), 2.0 * kPi * nu_over_c};
 }
 
 // ---- beam cube (a3) ------------------------------------------------------

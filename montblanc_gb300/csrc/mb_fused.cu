@@ -292,11 +292,11 @@ __device__ void load_sources(const FusedArgs<T>& A, int t, int ch, int s0, int n
 // the same FP64 value (split_f64) for the FP32 forms, whose phase is then
 // formed on the FP32 pipe (frac_cycles_df).
 template <typename T>
-__device__ __forceinline__ Cx<T> phase_term(const FusedArgs<T>& A, int t, int s, int a, T f, double nu_over_c) {
+__device__ __forceinline__ Cx<T> phase_term(const FusedArgs<T>& A, int t, int s, int a, T f, const NuC& nu) {
   double phi;
   const size_t e = (size_t(t) * A.nsrc + s) * A.na_glob + gant(A, a);
   if constexpr (sizeof(T) == 4) {
-    if (A.phi != nullptr) return phase_from_pair(__ldg(reinterpret_cast<const float2*>(A.phi) + e), nu_over_c);
+    if (A.phi != nullptr) return phase_from_pair(__ldg(reinterpret_cast<const float2*>(A.phi) + e), nu.p);
   }
   if (A.phi != nullptr) {
     phi = A.phi[e];
@@ -307,16 +307,16 @@ __device__ __forceinline__ Cx<T> phase_term(const FusedArgs<T>& A, int t, int s,
     phi = l * double(p[0]) + m * double(p[1]) + n * double(p[2]);
   }
   if (sizeof(T) == 8) return phase_from_phi<T>(phi, double(f));
-  return phase_from_cycles<T>(phi, nu_over_c);
+  return phase_from_cycles<T>(phi, nu.d);
 }
 
 // J(s, a) = E(s, a) . (K(s, a) sqrt(B)(s)) for one source and antenna.
 template <typename T>
 __device__ __forceinline__ Jones<T> compute_jones(const FusedArgs<T>& A, int t, int s, int a, const SrcInfo<T>& src,
-                                                  const AntInfo<T>& ai, T f, double nu_over_c,
+                                                  const AntInfo<T>& ai, T f, const NuC& nu,
                                                   const ChanPos<T>& cp, int plane_ch) {
   const BeamGeom G{A.lw, A.mh, A.nud};
-  Cx<T> K = phase_term(A, t, s, a, f, nu_over_c);
+  Cx<T> K = phase_term(A, t, s, a, f, nu);
   T l, m;
   beam_lm<T>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
   GridPos<T> gl = grid_pos<T>(l, A.ll, A.ul, A.lscale, A.lw);
@@ -335,10 +335,10 @@ template <typename T, bool DF = false>
 __device__ void produce_jones(const FusedArgs<T>& A, const SmemPlan& S, int t, int ch, int s0, int ns,
                               const SrcInfo<T>* ss, const AntInfo<T>* sa, Jones<T>* sJ, const ChanPos<T>& cp) {
   const T f = A.freq[ch];
-  const double nu_over_c = double(f) / kLightSpeed;
+  const NuC nu = make_nuc(double(f) / kLightSpeed);
   for (int i = threadIdx.x; i < ns * S.nap; i += blockDim.x) {
     int si = i / S.nap, a = i - si * S.nap;
-    const Jones<T> J = a < A.na ? compute_jones(A, t, s0 + si, a, ss[si], sa[a], f, nu_over_c, cp, ch)
+    const Jones<T> J = a < A.na ? compute_jones(A, t, s0 + si, a, ss[si], sa[a], f, nu, cp, ch)
                                 : jzero<T>();
     if constexpr (DF && sizeof(T) == 8) {  // per entry (re hi, im hi, re lo, im lo)
       const double* v = reinterpret_cast<const double*>(&J);
@@ -1118,13 +1118,13 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
   const uint32_t tmem = *tmem_slot;
 
   float fc[NCH], log2_ratio[NCH];
-  double nu_over_c[NCH];
+  NuC nu[NCH];
   ChanPos<float> cp[NCH];
 #pragma unroll
   for (int c = 0; c < NCH; ++c) {
     const int chc = min(ch + c, A.nchan - 1);
     fc[c] = A.freq[chc];
-    nu_over_c[c] = double(fc[c]) / kLightSpeed;
+    nu[c] = make_nuc(double(fc[c]) / kLightSpeed);
     cp[c] = chan_pos<float>(fc[c], A.lfreq, A.ufreq, A.nud);
     log2_ratio[c] = log2f(fc[c] / A.ref_freq[chc]);
   }
@@ -1176,7 +1176,7 @@ __global__ void __launch_bounds__(kTcThreads) coh_tc_fwd_kernel(FusedArgs<float>
           Jones<float> J = jzero<float>();
           if (a < A.na && sl < ns && c < nch) {
             if (PACK) src = point_source_info(A, t, ch + c, s0 + sl, log2_ratio[c]);
-            J = compute_jones(A, t, s0 + sl, a, src, sa[c * A.na + a], fc[c], nu_over_c[c], cp[c], ch + c);
+            J = compute_jones(A, t, s0 + sl, a, src, sa[c * A.na + a], fc[c], nu[c], cp[c], ch + c);
           }
           // row 2a holds J00, J01; row 2a + 1 holds J10, J11
           const Cx<float> r0a = i0 ? J.c : J.a, r0b = i0 ? J.d : J.b;
@@ -1567,10 +1567,10 @@ __device__ __forceinline__ void warp_keyed_add(T* acc, int first, int key, T (&v
 // l_over_n, m_over_n and B.
 template <typename T>
 __device__ __forceinline__ void chain_core(const FusedArgs<T>& A, int t, int ch, int s, int a, const SrcInfo<T>& src,
-                                           const AntInfo<T>& ai, const Jones<T>& gJ, T f, double nu_over_c,
+                                           const AntInfo<T>& ai, const Jones<T>& gJ, T f, const NuC& nu,
                                            T dphase, const ChanPos<T>& cp, T& gl0, T& gm0, Jones<T>& gB) {
   const BeamGeom G{A.lw, A.mh, A.nud};
-  Cx<T> K = phase_term(A, t, s, a, f, nu_over_c);
+  Cx<T> K = phase_term(A, t, s, a, f, nu);
   T l, m;
   beam_lm<T>(src.l, src.m, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
   GridPos<T> gl = grid_pos<T>(l, A.ll, A.ul, A.lscale, A.lw);
@@ -1626,11 +1626,10 @@ __device__ __forceinline__ void stokes_grads(const SrcInfo<T>& src, const Jones<
 // d chi^2 / d(l, m, I, Q, U, V, alpha) of source s.
 template <typename T>
 __device__ __forceinline__ void chain_item(const FusedArgs<T>& A, int t, int ch, int s, int a, const SrcInfo<T>& src,
-                                           const AntInfo<T>& ai, const Jones<T>& gJ, T f, double nu_over_c,
+                                           const AntInfo<T>& ai, const Jones<T>& gJ, T f, const NuC& nu, T dphase,
                                            T half_log_ratio, const ChanPos<T>& cp, T (&g)[7]) {
-  const T dphase = T(2.0 * kPi * nu_over_c);  // |dK/dphi|
   Jones<T> gB;
-  chain_core(A, t, ch, s, a, src, ai, gJ, f, nu_over_c, dphase, cp, g[0], g[1], gB);
+  chain_core(A, t, ch, s, a, src, ai, gJ, f, nu, dphase, cp, g[0], g[1], gB);
   T gs[5];
   stokes_grads(src, gB, half_log_ratio, gs);
 #pragma unroll
@@ -1643,7 +1642,8 @@ __device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int c
                           const SrcInfo<T>* ss, const AntInfo<T>* sa, const Jones<T>* sgJ,
                           T* sacc, const ChanPos<T>& cp) {
   const T f = A.freq[ch];
-  const double nu_over_c = double(f) / kLightSpeed;
+  const NuC nu = make_nuc(double(f) / kLightSpeed);
+  const T dphase = T(nu.dphase);  // |dK/dphi|
   const T half_log_ratio = T(0.5) * mb_log(f / A.ref_freq[ch]);
   const int n = ns * A.na;
   const int rounds = (n + blockDim.x - 1) / blockDim.x;
@@ -1653,7 +1653,7 @@ __device__ void adj_chain(const FusedArgs<T>& A, const SmemPlan& S, int t, int c
     const int si = active ? i / A.na : 0, a = active ? i - si * A.na : 0;
     T g[7] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
     if (active)
-      chain_item(A, t, ch, s0 + si, a, ss[si], sa[a], *jtile(sgJ, S, si, a), f, nu_over_c, half_log_ratio, cp, g);
+      chain_item(A, t, ch, s0 + si, a, ss[si], sa[a], *jtile(sgJ, S, si, a), f, nu, dphase, half_log_ratio, cp, g);
     warp_keyed_add<T, 7>(sacc, 0, active ? si : -1, g);
   }
 }
@@ -1670,7 +1670,8 @@ __device__ void adj_ext_tile(const FusedArgs<T>& A, const SmemPlan& S, int t, in
                              const SrcInfo<T>* ss, const AntInfo<T>* sa, const Jones<T>* sJ, const Jones<T>* sX,
                              T* sacc, T kg, T ks, const ChanPos<T>& cp) {
   const T f = A.freq[ch];
-  const double nu_over_c = double(f) / kLightSpeed;
+  const NuC nu = make_nuc(double(f) / kLightSpeed);
+  const T dphase = T(nu.dphase);  // |dK/dphi|
   const T half_log_ratio = T(0.5) * mb_log(f / A.ref_freq[ch]);
   const int n = ns * A.na;
   const int rounds = (n + blockDim.x - 1) / blockDim.x;
@@ -1697,7 +1698,7 @@ __device__ void adj_ext_tile(const FusedArgs<T>& A, const SmemPlan& S, int t, in
         }
       }
       T gc7[7];
-      chain_item(A, t, ch, s0 + si, a, src, sa[a], acc, f, nu_over_c, half_log_ratio, cp, gc7);
+      chain_item(A, t, ch, s0 + si, a, src, sa[a], acc, f, nu, dphase, half_log_ratio, cp, gc7);
 #pragma unroll
       for (int e = 0; e < 7; ++e) g[e] = gc7[e];
     }
@@ -2065,9 +2066,9 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
     const bool ant_ok = a < A.na && c < nch;
     const AntInfo<float> ai = sa[c * A.na + (ant_ok ? a : 0)];
     const float f = A.freq[chl];
-    const double nu_over_c = double(f) / kLightSpeed;
+    const NuC nu = make_nuc(double(f) / kLightSpeed);
     const ChanPos<float> cp = chan_pos<float>(f, A.lfreq, A.ufreq, A.nud);
-    const float dphase = float(2.0 * kPi * nu_over_c);
+    const float dphase = float(nu.dphase);
     unsigned char* hi = stage + size_t(grp) * kJopBytes;
     unsigned char* lo = hi + kJopBytes / 2;
     const BeamGeom G{A.lw, A.mh, A.nud};
@@ -2121,7 +2122,7 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
         if (!bad && ant_ok && sl < ns) {
           const int sg = s0 + sl;
           const float4 tb = tsrc[sl].b, tlm = tsrc[sl].lm;
-          const Cx<float> K = phase_term(A, t, sg, a, f, nu_over_c);
+          const Cx<float> K = phase_term(A, t, sg, a, f, nu);
           float l, m;
           beam_lm<float>(tlm.x, tlm.y, ai.sin_pa, ai.cos_pa, ai.pe_l, ai.pe_m, ai.sc_l, ai.sc_m, l, m);
           const GridPos<float> gl = grid_pos<float>(l, A.ll, A.ul, A.lscale, A.lw);
