@@ -48,15 +48,15 @@ NCU_LIMITER = {
     'coh_tc_adj_kernel': {
         'source': 'profiles/coh_tc_adj_kernel_profile_point.md',
         'limiter': 'CUDA-core issue and latency of the per-(source, antenna) producer and chain',
-        'sm__pipe_tensor_cycles_active': 0.101, 'smsp__issue_active': 0.425,
-        'pipe_fma': 0.212, 'pipe_alu': 0.265, 'pipe_fp64': 0.058, 'pipe_xu': 0.045,
-        'thread_instructions_per_item': 792},
+        'sm__pipe_tensor_cycles_active': 0.115, 'smsp__issue_active': 0.392,
+        'pipe_fma_cycles': 0.246, 'pipe_alu': 0.284, 'pipe_fp64': 0.018, 'pipe_xu': 0.034,
+        'thread_instructions_per_item': 647},
     'coh_tc_fwd_kernel': {
         'source': 'profiles/coh_tc_fwd_kernel_profile_point.md',
         'limiter': 'CUDA-core issue and latency of the per-(source, antenna) producer; TMEM drains',
-        'sm__pipe_tensor_cycles_active': 0.295, 'smsp__issue_active': 0.453,
-        'pipe_fma': 0.167, 'pipe_alu': 0.354, 'pipe_fp64': 0.073, 'pipe_xu': 0.040,
-        'thread_instructions_per_item': 634},
+        'sm__pipe_tensor_cycles_active': 0.352, 'smsp__issue_active': 0.436,
+        'pipe_fma_cycles': 0.204, 'pipe_alu': 0.345, 'pipe_fp64': 0.003, 'pipe_xu': 0.048,
+        'thread_instructions_per_item': 510},
 }
 
 # DRAM bytes per launch from a one-kernel ncu capture on the profile_point
@@ -67,10 +67,10 @@ NCU_LIMITER = {
 # time step run together and share them in L2).
 NCU_DRAM = {
     # kernel: (bytes per unit, bytes per (time, source, antenna)); the
-    # profile_point launch moved 337.5 MB (forward) and 217.6 MB (adjoint)
-    # over 2048 units and 32 x 4050 x 64 FP64 path lengths (66.4 MB)
-    'coh_tc_fwd_kernel': (145.1e3, 8.0),
-    'coh_tc_adj_kernel': (73.8e3, 8.0),
+    # profile_point launch moved 475.5 MB (forward) and 221.6 MB (adjoint)
+    # over 2048 units and 32 x 4050 x 64 8-byte path lengths (66.4 MB)
+    'coh_tc_fwd_kernel': (199.7e3, 8.0),
+    'coh_tc_adj_kernel': (75.8e3, 8.0),
 }
 
 
