@@ -100,7 +100,7 @@ def chunk_bytes(nt, nc, na, nbl, nsrc, ft_bytes, weights):
     b += nt * (na * (3 + 1) * ft_bytes + 2 * nbl * 4)     # uvw, pa, antenna pairs
     b += nsrc * nt * 5 * ft_bytes                         # stokes, alpha
     b += nt * nbl * nc * ft_bytes                         # chi^2 terms
-    b += nt * nsrc * na * 8                               # FP64 phase path lengths
+    b += nt * nsrc * na * 8                               # path lengths (8 bytes each)
     b += nt * nc * 8 + (1 << 16)
     return b
 

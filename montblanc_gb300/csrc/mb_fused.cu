@@ -2289,7 +2289,7 @@ __global__ void __launch_bounds__(kTaThreads, 1) coh_tc_adj_kernel(FusedArgs<flo
 }
 
 // ---------------------------------------------------------------------------
-// Small kernels: FP64 phase path lengths, gradient finalisation
+// Small kernels: phase path lengths, gradient finalisation
 // ---------------------------------------------------------------------------
 // Frequency-blended beam plane per active channel as bilinear coefficients
 // per (l, m) cell (see plane_cell), formed in FP64 from the cube.
@@ -2605,8 +2605,9 @@ mb_status check_inputs(const mb_dims* d, const mb_props* P, uint32_t options, co
   return MB_OK;
 }
 
-// Per-call tables shared by the forward and the adjoint: FP64 path lengths,
-// the frequency-blended beam plane, and (FP32) sqrt(B) at the reference
+// Per-call tables shared by the forward and the adjoint: the path lengths
+// (formed in FP64; stored as FP32 pairs for the FP32 kernels), the
+// frequency-blended beam plane, and (FP32) sqrt(B) at the reference
 // frequency.
 template <typename T>
 mb_status launch_prep(const FusedArgs<T>& A, void* ws, const WsLayout& L, cudaStream_t stream) {

@@ -56,7 +56,7 @@ struct FusedArgs {
   // CUDA-core launch before it has left their sums in vis_in).
   bool tc_ext;
   // workspace
-  const double* phi;  // (ntime, nsrc, na) FP64 phase path lengths
+  const double* phi;  // (ntime, nsrc, na) path lengths: FP64, or FP32 (hi, lo) pairs in FP32 kernels
   const T* plane;     // (nchan, beam_lw, beam_mh, 12) frequency-blended beam, or NULL
   const T* bsq0;      // (nsrc, ntime, 8) sqrt(B) at nu = nu_ref and alpha / 2, or NULL
   double* partial;    // (ntime * nchan) chi^2 partial sums
