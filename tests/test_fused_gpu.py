@@ -114,3 +114,31 @@ def test_kernel_timer_reports_the_fused_launches():
     assert kt.launches == sum(n for _, n in times.values())
     assert all(ms >= 0.0 for ms, _ in times.values())
     assert abs(x2 - ref['X2']) <= TOL['float']['X2'] * abs(ref['X2'])
+
+
+@pytest.mark.parametrize('mode', ['native', 'split_tf32'])
+def test_fp32_phase_on_long_baselines(mode):
+    """Baselines thousands of kilometres long (about 2e6 phase cycles): the
+    FP32 forms reduce phi nu / c from FP32 pairs of the FP64 path length, and
+    their model visibilities keep their usual error against the FP64 oracle
+    (a phase argument formed in FP32 would be off by whole cycles here)."""
+    from montblanc_gb300 import synth
+    from montblanc_gb300.rime import RimeProblem
+    from test_units_gpu import norm_err
+    P = synth.make_problem(ntime=2, na=12, nchan=4, npsrc=10, seed=5, beam_shape=(12, 12, 6))
+    P['uvw'] = P['uvw'] * 5000.0
+    # inputs representable in FP32, so that both see the same values
+    for k, v in P.items():
+        if isinstance(v, np.ndarray) and v.dtype == np.float64:
+            P[k] = v.astype(np.float32).astype(np.float64)
+        elif isinstance(v, np.ndarray) and v.dtype == np.complex128:
+            P[k] = v.astype(np.complex64).astype(np.complex128)
+    l, m = P['lm'][:, 0], P['lm'][:, 1]
+    phi = (P['uvw'][..., 0][:, None] * l[None, :, None] + P['uvw'][..., 1][:, None] * m[None, :, None] +
+           P['uvw'][..., 2][:, None] * (np.sqrt(1 - l * l - m * m) - 1)[None, :, None])
+    assert np.abs(phi).max() * P['frequency'].max() / 299792458.0 > 1e6
+    ref_vis, _, _ = O.forward(P)
+    prob = RimeProblem.from_numpy(P, dtype='float')
+    vis = prob.empty_vis()
+    prob.forward(mode=mode, model_vis=vis)
+    assert norm_err(vis.cpu().numpy(), ref_vis) < 1e-6
