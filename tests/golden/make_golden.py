@@ -210,8 +210,8 @@ def _batch_vis(args):
 
 
 def reference_outputs_batched(P, batch=256, processes=None):
-    """The reference's forward over source batches (SURVEY-style chunking
-    of CPUSolver: the sum over sources is linear and G is applied after it):
+    """The reference's forward over source batches (CPUSolver chunked over
+    sources: the sum over sources is linear and G is applied after it):
     compute_ekb_vis per batch, summed, then compute_gekb_vis,
     compute_chi_sqrd_sum_terms and compute_chi_sqrd on the sum."""
     nsrc = P['lm'].shape[0]
